@@ -1,0 +1,192 @@
+/*
+ * scft.h -- C ABI of libscft (scft_gb300): the SCFT inner loop of giantsda/SCFT
+ * (field w -> FEM propagator q -> density phi -> residual -> Anderson/Broyden
+ * update of w) on one GB300 GPU.
+ *
+ * All entry points return int status codes (SCFT_OK = 0, negative = error) and
+ * never throw.  Host buffers are owned by the caller; device memory is owned by
+ * the library.  The drop-in entry points keep the reference's argument meaning
+ * and indexing; each cites the reference function it replaces.
+ */
+#ifndef SCFT_H
+#define SCFT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SCFT_OK 0
+#define SCFT_EINVAL (-1)    /* invalid argument */
+#define SCFT_ECUDA (-2)     /* CUDA runtime error */
+#define SCFT_ENOMEM (-3)    /* device or host allocation failed */
+#define SCFT_ENOCONFIG (-4) /* scft_set_config was not called */
+#define SCFT_ENODEV (-5)    /* no CUDA device */
+#define SCFT_ESINGULAR (-6) /* singular Jacobian (Broyden) */
+
+/* ---- per-instance result status bits ---- */
+#define SCFT_ST_NOT_DOMINANT 1 /* 1 + ds*w < 0 somewhere: system lost diagonal dominance */
+#define SCFT_ST_NONFINITE 2    /* non-finite density: instance stopped */
+#define SCFT_ST_CONVERGED 4
+#define SCFT_ST_MAXIT 8
+#define SCFT_ST_RESTARTED 16   /* the Anderson history was restarted at least once */
+#define SCFT_ST_WATCHDOG 32    /* the host loop stopped on its launch cap */
+
+enum { SCFT_RULE_ROMBERG = 0, SCFT_RULE_TRAPEZOID = 1 };
+enum { SCFT_F32 = 0, SCFT_F64 = 1 };
+enum { SCFT_MIX_LINEAR = 0, SCFT_MIX_LOG = 1 };
+
+/* =========================================================================
+ * Drop-in single-instance path (the reference's process globals become one
+ * configuration set by scft_set_config).
+ * ========================================================================= */
+
+typedef struct scft_config {
+  int n_nodes;       /* total nodes N+2 (1D_FEM.c:50 adds the two walls) */
+  const double *x;   /* n_nodes coordinates, or NULL for uniform on [0, L] (1D_FEM.c:61) */
+  double L;          /* film width (1D_FEM.c:61: 3.72374) */
+  const double *f0;  /* n_nodes target density (the global f0_given, 1D_FEM.c:14) */
+  int nsteps;        /* contour steps (1D_FEM.c:60 runs 2049 steps of ds = 1/2048) */
+  double ds;         /* contour step */
+  int rule;          /* SCFT_RULE_ROMBERG (romint.c:21) or SCFT_RULE_TRAPEZOID (.m:119-124) */
+  int sign;          /* +1: out = phi - f0 (1D_FEM.c:276); -1: out = f0 - phi (drivescft.cc:212) */
+  int precision;     /* SCFT_F64 (default) or SCFT_F32 */
+} scft_config;
+
+/* Defaults of the drop-in: 2049 steps of ds = 1/2048 with the trapezoid rule
+   (the MATLAB prototype's reading of 1D_FEM.c:60-61,208), sign +1, FP64. */
+void scft_config_init(scft_config *c);
+
+/* Sets the problem the drop-in residual evaluates (replaces the globals
+   f0_given / L / total_time_step of 1D_FEM.c:13-14,60-61).  Copies the arrays. */
+int scft_set_config(const scft_config *c);
+
+/* Replaces simple_FEM_1D_transient (1D_FEM.c:47-287): n_interior = N-2 interior
+   nodes, w and out are 1-based NR vectors (w[1..n_interior] read,
+   out[1..n_interior] written).  Returns SCFT_OK or an error code. */
+int scft_fem_residual(int n_interior, double *w, double *out);
+
+/* The same evaluation with the void(int, double*, double*) callback type the
+   reference's solvers take: 1-based (broydn.c:44, adm.c with flag=1) ... */
+void scft_fem_residual_vf(int n_interior, double *w, double *out);
+/* ... and 0-based (ADM_chen_C.c:18 / SCFT_wrapper without BROYDN, drivescft.cc:218-234). */
+void scft_fem_residual0_vf(int n_interior, double *w, double *out);
+/* Fixed-point form for adm (adm.c:16-21 solves x = f(x)): out = w + (phi - f0), 1-based. */
+void scft_fem_fixedpoint_vf(int n_interior, double *w, double *out);
+
+/* Density and partition function of the configured problem for a full nodal
+   field w_nodes[0..n_nodes-1] (walls ignored).  phi: n_nodes, Q: optional. */
+int scft_density(const double *w_nodes, double *phi, double *Q);
+
+/* Last error message of the calling thread (never NULL). */
+const char *scft_last_error(void);
+const char *scft_strerror(int code);
+
+/* ---- the reference's solvers, mixing on the GPU ---- */
+
+typedef void (*scft_vecfunc)(int n, double *in, double *out);
+
+/* Replaces adm (adm.c:24-313): Anderson mixing for x = f(x); flag 0: x[0..n-1],
+   flag 1: x[1..n].  *check = 0 converged (|f(x)-x|_inf < 1e-10), 1 not.
+   f == scft_fem_fixedpoint_vf keeps every evaluation on the device.
+   Returns SCFT_OK or an error code. */
+int scft_adm(double *x, int n, int *check, scft_vecfunc f, int flag);
+/* Iteration cap of scft_adm (the reference's MAXITS, adm.c:5: 1000000). */
+void scft_adm_set_maxit(int maxit);
+
+/* Replaces adm_chen (DEALII_SCFT/src/ADM_chen_C.c:18-147): Anderson mixing for
+   F(x) = 0, 0-based.  Returns 0 solved, 1 not solved, 2 NaN residual, <0 error.
+   f == scft_fem_residual0_vf keeps every evaluation on the device. */
+int scft_adm_chen(scft_vecfunc f, double *x, double tol, int maxit, int n, double lmd, int nn,
+                  int final_);
+
+/* Replaces broydn (broydn.c:44-292; fdjac/lnsrch/qrdcmp/qrupdt/rsolv/rotate of
+   DEALII_SCFT/src): x 1-based, *check as broydn sets it.  The tolerance is the
+   reference's global err (set with scft_broydn_set_tol, read back the reached
+   error with scft_broydn_get_err).  With f == scft_fem_residual_vf the
+   finite-difference Jacobian's n evaluations run as one batched launch. */
+int scft_broydn(double *x, int n, int *check, scft_vecfunc f);
+void scft_broydn_set_tol(double tol);
+double scft_broydn_get_err(void);
+
+/* =========================================================================
+ * Batched path: thousands of independent instances per launch.
+ * ========================================================================= */
+
+typedef struct scft_instance {
+  int n_nodes;        /* elements + 1 */
+  const double *x;    /* n_nodes coordinates or NULL (uniform on [0, L]) */
+  double L;
+  const double *f0;   /* n_nodes target density */
+  const double *w0;   /* n_nodes initial field or NULL (zero); wall values ignored */
+  int nsteps;
+  double ds;
+  int rule;           /* SCFT_RULE_* */
+} scft_instance;
+
+typedef struct scft_solve_opts {
+  int precision;      /* SCFT_F32 (propagator in FP32, mixing/residual FP64) or SCFT_F64 */
+  double tol;         /* ||phi - f0||_inf target */
+  double tol32_factor;/* FP32 iterations stop at tol * tol32_factor */
+  int verify64;       /* FP32-converged instances are re-evaluated once in FP64 */
+  int maxit;
+  int depth;          /* Anderson history depth (<= 16) */
+  double beta;        /* mixing parameter */
+  double clip;        /* max-norm bound on one field update */
+  double grow;        /* restart the history when the error grows by this factor */
+  double reg;         /* relative Tikhonov term of the least-squares solve */
+  int residual_mode;  /* SCFT_MIX_LINEAR (phi - f0) or SCFT_MIX_LOG (ln phi - ln f0) */
+  double precond;     /* a in (1 - a d2/dx2) applied to the mixing residual */
+  int iters_per_graph;/* iterations captured in one CUDA graph */
+} scft_solve_opts;
+
+typedef struct scft_result {
+  int status;         /* SCFT_ST_* bits */
+  int iterations;
+  double err;         /* ||phi - f0||_inf at the last evaluation */
+  double Q;
+} scft_result;
+
+typedef struct scft_batch scft_batch;
+
+void scft_solve_opts_init(scft_solve_opts *o);
+
+/* Copies the instances to the device.  Returns SCFT_OK and *out, or an error. */
+int scft_batch_create(const scft_instance *inst, int count, scft_batch **out);
+/* Overwrite all fields (concatenated n_nodes values per instance). */
+int scft_batch_set_fields(scft_batch *b, const double *w_nodes);
+/* One propagator pass at the current fields (density and Q for every instance). */
+int scft_batch_evaluate(scft_batch *b, int precision);
+/* Solve every instance to opts->tol; res (count entries) may be NULL. */
+int scft_batch_solve(scft_batch *b, const scft_solve_opts *opts, scft_result *res);
+/* Copy fields / densities (concatenated n_nodes per instance) and Q out; any may be NULL. */
+int scft_batch_get(scft_batch *b, double *w_nodes, double *phi_nodes, double *Q);
+/* Restore every field to the w0 given at creation (device copy, no host traffic). */
+int scft_batch_reset(scft_batch *b);
+/* Device time of the last scft_batch_evaluate / scft_batch_solve / scft_batch_reset,
+   measured with CUDA events on the batch's stream (ms). */
+double scft_batch_last_ms(scft_batch *b);
+/* Per shape class of precision p: nodes per thread, warps per instance, instance
+   count, algorithmic half-contour bytes of one pass (write + read of slices
+   0..nsteps/2 of every node, 4 or 8 bytes each) and the event-timed duration (ms)
+   of one pass of that class alone.  Writes at most max_classes entries and
+   returns the number of classes (or an error code). */
+int scft_batch_profile(scft_batch *b, int precision, int max_classes, int *C, int *NW, int *items,
+                       double *bytes, double *ms);
+/* Per-instance status bits of the last evaluate/solve (count ints). */
+int scft_batch_status(scft_batch *b, int *status);
+/* Choose the propagator shape of one instance: C nodes per thread (1,2,4,8) and
+   NW warps per instance (1..32); C = 0 restores the default. */
+int scft_batch_set_shape(scft_batch *b, int precision, int index, int C, int NW);
+/* Time the candidate shapes of each (size, precision) bucket on this batch and
+   keep the fastest (the autotuner). */
+int scft_batch_autotune(scft_batch *b, int precision);
+int scft_batch_destroy(scft_batch *b);
+
+/* Kernels launched by this library since load (graph replays count each node). */
+long long scft_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

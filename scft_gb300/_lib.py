@@ -1,0 +1,127 @@
+"""ctypes declarations of libscft.so (the C ABI in include/scft.h).
+
+The library is built in-tree by ``scft_gb300.build`` (``__graft_entry__.build()``).
+Loading fails loudly when it is missing: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libscft.so")
+
+SCFT_OK = 0
+SCFT_EINVAL = -1
+SCFT_ECUDA = -2
+SCFT_ENOMEM = -3
+SCFT_ENOCONFIG = -4
+SCFT_ENODEV = -5
+SCFT_ESINGULAR = -6
+
+ST_NOT_DOMINANT = 1
+ST_NONFINITE = 2
+ST_CONVERGED = 4
+ST_MAXIT = 8
+ST_RESTARTED = 16
+ST_WATCHDOG = 32
+
+RULE_ROMBERG, RULE_TRAPEZOID = 0, 1
+F32, F64 = 0, 1
+MIX_LINEAR, MIX_LOG = 0, 1
+
+_dp = C.POINTER(C.c_double)
+VECFUNC = C.CFUNCTYPE(None, C.c_int, _dp, _dp)
+
+
+class ScftConfig(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("x", _dp), ("L", C.c_double), ("f0", _dp),
+                ("nsteps", C.c_int), ("ds", C.c_double), ("rule", C.c_int), ("sign", C.c_int),
+                ("precision", C.c_int)]
+
+
+class ScftInstance(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("x", _dp), ("L", C.c_double), ("f0", _dp), ("w0", _dp),
+                ("nsteps", C.c_int), ("ds", C.c_double), ("rule", C.c_int)]
+
+
+class ScftSolveOpts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("tol", C.c_double), ("tol32_factor", C.c_double),
+                ("verify64", C.c_int), ("maxit", C.c_int), ("depth", C.c_int), ("beta", C.c_double),
+                ("clip", C.c_double), ("grow", C.c_double), ("reg", C.c_double),
+                ("residual_mode", C.c_int), ("precond", C.c_double), ("iters_per_graph", C.c_int)]
+
+
+class ScftResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("err", C.c_double), ("Q", C.c_double)]
+
+
+# name -> (restype, argtypes); every function declared in include/scft.h
+SIGNATURES = {
+    "scft_config_init": (None, [C.POINTER(ScftConfig)]),
+    "scft_set_config": (C.c_int, [C.POINTER(ScftConfig)]),
+    "scft_fem_residual": (C.c_int, [C.c_int, _dp, _dp]),
+    "scft_fem_residual_vf": (None, [C.c_int, _dp, _dp]),
+    "scft_fem_residual0_vf": (None, [C.c_int, _dp, _dp]),
+    "scft_fem_fixedpoint_vf": (None, [C.c_int, _dp, _dp]),
+    "scft_density": (C.c_int, [_dp, _dp, _dp]),
+    "scft_last_error": (C.c_char_p, []),
+    "scft_strerror": (C.c_char_p, [C.c_int]),
+    "scft_adm": (C.c_int, [_dp, C.c_int, C.POINTER(C.c_int), C.c_void_p, C.c_int]),
+    "scft_adm_set_maxit": (None, [C.c_int]),
+    "scft_adm_chen": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int,
+                                C.c_int]),
+    "scft_broydn": (C.c_int, [_dp, C.c_int, C.POINTER(C.c_int), C.c_void_p]),
+    "scft_broydn_set_tol": (None, [C.c_double]),
+    "scft_broydn_get_err": (C.c_double, []),
+    "scft_solve_opts_init": (None, [C.POINTER(ScftSolveOpts)]),
+    "scft_batch_create": (C.c_int, [C.POINTER(ScftInstance), C.c_int, C.POINTER(C.c_void_p)]),
+    "scft_batch_set_fields": (C.c_int, [C.c_void_p, _dp]),
+    "scft_batch_evaluate": (C.c_int, [C.c_void_p, C.c_int]),
+    "scft_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(ScftSolveOpts), C.POINTER(ScftResult)]),
+    "scft_batch_get": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "scft_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "scft_batch_reset": (C.c_int, [C.c_void_p]),
+    "scft_batch_last_ms": (C.c_double, [C.c_void_p]),
+    "scft_batch_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int), _dp, _dp]),
+    "scft_batch_set_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "scft_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
+    "scft_batch_destroy": (C.c_int, [C.c_void_p]),
+    "scft_kernel_launches": (C.c_longlong, []),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libscft.so (once).  Raises ImportError when it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"libscft.so not found at {p}: run __graft_entry__.build() "
+                          "(python -m scft_gb300.build); there is no CPU fallback")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class ScftError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        lib = load()
+        msg = lib.scft_last_error().decode() or lib.scft_strerror(code).decode()
+        super().__init__(f"{where}: {msg} (code {code})")
+        self.code = code
+
+
+def check(code: int, where: str) -> int:
+    if code < 0:
+        raise ScftError(code, where)
+    return code

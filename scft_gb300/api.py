@@ -1,0 +1,275 @@
+"""Host-side mirror of the reference's SCFT interface, over the C ABI.
+
+* ``simple_FEM_1D_transient(N, w, out)``  -- 1D_FEM.c:47 (1-based arrays)
+* ``adm(x, n, f, flag)``                   -- adm.c:24
+* ``adm_chen(f, x, tol, maxit, n, lmd, nn, final)`` -- ADM_chen_C.c:18
+* ``broydn(x, n, f, tol)``                 -- broydn.c:44 (tolerance = the global err)
+* ``Batch``                                -- thousands of instances per launch
+
+The callbacks the solvers accept are either Python callables ``f(x) -> out``
+(0-based numpy arrays) or one of the library's own evaluators
+(``FEM_RESIDUAL``, ``FEM_RESIDUAL0``, ``FEM_FIXEDPOINT``), which keep every
+evaluation on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check
+
+
+def _dp(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class _Native:
+    """Marker for the library's own C callbacks."""
+
+    def __init__(self, name: str, base: int):
+        self.name = name
+        self.base = base
+
+    def pointer(self):
+        return C.cast(getattr(L.load(), self.name), C.c_void_p)
+
+
+FEM_RESIDUAL = _Native("scft_fem_residual_vf", 1)     # 1-based, broydn / adm(flag=1) form
+FEM_RESIDUAL0 = _Native("scft_fem_residual0_vf", 0)   # 0-based, adm_chen form
+FEM_FIXEDPOINT = _Native("scft_fem_fixedpoint_vf", 1) # x + (phi - f0), adm form
+
+
+def _callback(f, base: int):
+    """Return (void* function pointer, keep-alive) for a solver callback."""
+    if isinstance(f, _Native):
+        return f.pointer(), None
+
+    def cb(n, xp, op):
+        x = np.ctypeslib.as_array(xp, shape=(n + base,))[base:].copy()
+        np.ctypeslib.as_array(op, shape=(n + base,))[base:] = np.asarray(f(x), dtype=np.float64)
+
+    c = L.VECFUNC(cb)
+    return C.cast(c, C.c_void_p), c
+
+
+# ---------------------------------------------------------------------------
+# drop-in single instance
+# ---------------------------------------------------------------------------
+_config_keep: list = []
+
+
+def set_config(f0, L_width=None, x=None, nsteps=2049, ds=1.0 / 2048, rule=L.RULE_TRAPEZOID, sign=1,
+               precision=L.F64):
+    """Configure the problem that simple_FEM_1D_transient evaluates (the reference's
+    globals f0_given, L and total_time_step)."""
+    lib = L.load()
+    f0 = np.ascontiguousarray(f0, dtype=np.float64)
+    xa = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+    cfg = L.ScftConfig()
+    lib.scft_config_init(C.byref(cfg))
+    cfg.n_nodes = len(f0)
+    cfg.x = _dp(xa)
+    cfg.L = float(L_width if L_width is not None else (xa[-1] - xa[0]))
+    cfg.f0 = _dp(f0)
+    cfg.nsteps = int(nsteps)
+    cfg.ds = float(ds)
+    cfg.rule = int(rule)
+    cfg.sign = int(sign)
+    cfg.precision = int(precision)
+    check(lib.scft_set_config(C.byref(cfg)), "scft_set_config")
+    _config_keep[:] = [f0, xa]
+
+
+def simple_FEM_1D_transient(N: int, w: np.ndarray, out: np.ndarray) -> int:
+    """Drop-in for simple_FEM_1D_transient(int N, double* w, double* out)
+    (1D_FEM.c:47-287): N interior nodes, w[1..N] read, out[1..N] written."""
+    lib = L.load()
+    if len(w) < N + 1 or len(out) < N + 1:
+        raise ValueError("1-based arrays need N+1 entries")
+    return check(lib.scft_fem_residual(int(N), _dp(w), _dp(out)), "simple_FEM_1D_transient")
+
+
+def fem_residual(w_interior: np.ndarray) -> np.ndarray:
+    """0-based convenience form of the drop-in residual."""
+    w = np.concatenate([[0.0], np.asarray(w_interior, dtype=np.float64)])
+    out = np.zeros_like(w)
+    simple_FEM_1D_transient(len(w) - 1, w, out)
+    return out[1:]
+
+
+def density(w_nodes: np.ndarray):
+    lib = L.load()
+    w = np.ascontiguousarray(w_nodes, dtype=np.float64)
+    phi = np.empty_like(w)
+    Q = C.c_double()
+    check(lib.scft_density(_dp(w), _dp(phi), C.byref(Q)), "scft_density")
+    return phi, Q.value
+
+
+# ---------------------------------------------------------------------------
+# solvers
+# ---------------------------------------------------------------------------
+def adm(x, n, f, flag=0, maxit=1000000):
+    """adm.c:24: Anderson mixing for x = f(x).  Returns (x, check)."""
+    lib = L.load()
+    xx = np.ascontiguousarray(np.concatenate([[0.0] * flag, np.asarray(x, dtype=np.float64)]))
+    fp, keep = _callback(f, flag)
+    chk = C.c_int(1)
+    lib.scft_adm_set_maxit(int(maxit))
+    check(lib.scft_adm(_dp(xx), int(n), C.byref(chk), fp, int(flag)), "scft_adm")
+    del keep
+    return xx[flag:], chk.value
+
+
+def adm_chen(f, x, tol, maxit, n, lmd, nn, final=False):
+    """ADM_chen_C.c:18: Anderson mixing for F(x) = 0.  Returns (status, x)."""
+    lib = L.load()
+    xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).copy())
+    fp, keep = _callback(f, 0)
+    rc = check(lib.scft_adm_chen(fp, _dp(xx), float(tol), int(maxit), int(n), float(lmd), int(nn),
+                                 int(bool(final))), "scft_adm_chen")
+    del keep
+    return rc, xx
+
+
+def broydn(x, n, f, tol):
+    """broydn.c:44 with the global err = tol.  Returns (x, check, err)."""
+    lib = L.load()
+    xx = np.ascontiguousarray(np.concatenate([[0.0], np.asarray(x, dtype=np.float64)]))
+    fp, keep = _callback(f, 1)
+    chk = C.c_int(1)
+    lib.scft_broydn_set_tol(float(tol))
+    check(lib.scft_broydn(_dp(xx), int(n), C.byref(chk), fp), "scft_broydn")
+    del keep
+    return xx[1:], chk.value, lib.scft_broydn_get_err()
+
+
+# ---------------------------------------------------------------------------
+# batched path
+# ---------------------------------------------------------------------------
+def solve_opts(**kw) -> L.ScftSolveOpts:
+    o = L.ScftSolveOpts()
+    L.load().scft_solve_opts_init(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+class Batch:
+    """Independent SCFT instances solved together on the GPU.
+
+    ``instances`` is a sequence of dicts with keys n_nodes, L, f0, nsteps, ds and
+    optional x, w0, rule."""
+
+    def __init__(self, instances):
+        self.lib = L.load()
+        self.count = len(instances)
+        self._keep = []
+        arr = (L.ScftInstance * self.count)()
+        self.n_nodes = np.empty(self.count, dtype=np.int64)
+        for i, d in enumerate(instances):
+            f0 = np.ascontiguousarray(d["f0"], dtype=np.float64)
+            x = None if d.get("x") is None else np.ascontiguousarray(d["x"], dtype=np.float64)
+            w0 = None if d.get("w0") is None else np.ascontiguousarray(d["w0"], dtype=np.float64)
+            self._keep += [f0, x, w0]
+            s = arr[i]
+            s.n_nodes = int(d["n_nodes"])
+            s.x = _dp(x)
+            s.L = float(d.get("L", 0.0))
+            s.f0 = _dp(f0)
+            s.w0 = _dp(w0)
+            s.nsteps = int(d["nsteps"])
+            s.ds = float(d["ds"])
+            s.rule = int(d.get("rule", L.RULE_ROMBERG))
+            self.n_nodes[i] = s.n_nodes
+        self.offsets = np.concatenate([[0], np.cumsum(self.n_nodes)])
+        h = C.c_void_p()
+        check(self.lib.scft_batch_create(arr, self.count, C.byref(h)), "scft_batch_create")
+        self._keep = []
+        self.h = h
+
+    def split(self, flat):
+        return [flat[self.offsets[i]:self.offsets[i + 1]] for i in range(self.count)]
+
+    def set_fields(self, w_nodes_list):
+        flat = np.ascontiguousarray(np.concatenate(w_nodes_list), dtype=np.float64)
+        check(self.lib.scft_batch_set_fields(self.h, _dp(flat)), "scft_batch_set_fields")
+
+    def evaluate(self, precision=L.F64):
+        check(self.lib.scft_batch_evaluate(self.h, int(precision)), "scft_batch_evaluate")
+
+    def solve(self, opts: L.ScftSolveOpts | None = None, **kw):
+        o = opts if opts is not None else solve_opts(**kw)
+        res = (L.ScftResult * self.count)()
+        check(self.lib.scft_batch_solve(self.h, C.byref(o), res), "scft_batch_solve")
+        return {
+            "status": np.array([r.status for r in res]),
+            "iterations": np.array([r.iterations for r in res]),
+            "err": np.array([r.err for r in res]),
+            "Q": np.array([r.Q for r in res]),
+        }
+
+    def get(self):
+        tot = int(self.offsets[-1])
+        w = np.empty(tot)
+        phi = np.empty(tot)
+        Q = np.empty(self.count)
+        check(self.lib.scft_batch_get(self.h, _dp(w), _dp(phi), _dp(Q)), "scft_batch_get")
+        return self.split(w), self.split(phi), Q
+
+    def status(self):
+        st = (C.c_int * self.count)()
+        check(self.lib.scft_batch_status(self.h, st), "scft_batch_status")
+        return np.array(st[:])
+
+    def reset(self):
+        """Restore the creation-time fields on the device."""
+        check(self.lib.scft_batch_reset(self.h), "scft_batch_reset")
+
+    def last_ms(self) -> float:
+        """Event-timed device duration of the last evaluate / solve / reset."""
+        return float(self.lib.scft_batch_last_ms(self.h))
+
+    def profile(self, precision=L.F32, max_classes=64):
+        """Per shape class: (C, NW, items, algorithmic bytes, ms) of one pass alone."""
+        n = max_classes
+        Cs, NWs, its = (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+        by, ms = (C.c_double * n)(), (C.c_double * n)()
+        k = check(self.lib.scft_batch_profile(self.h, int(precision), n, Cs, NWs, its, by, ms),
+                  "scft_batch_profile")
+        return [dict(C=Cs[i], NW=NWs[i], items=its[i], bytes=by[i], ms=ms[i]) for i in range(min(k, n))]
+
+    def set_shape(self, precision, index, C_nodes, NW):
+        check(self.lib.scft_batch_set_shape(self.h, int(precision), int(index), int(C_nodes), int(NW)),
+              "scft_batch_set_shape")
+
+    def autotune(self, precision=L.F32):
+        check(self.lib.scft_batch_autotune(self.h, int(precision)), "scft_batch_autotune")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.scft_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def kernel_launches() -> int:
+    return int(L.load().scft_kernel_launches())

@@ -1,0 +1,47 @@
+// common.cuh -- shared device/host definitions of the scft_gb300 runtime.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace scft {
+
+// Per-instance batch arrays (struct of arrays, device pointers).  Node arrays of
+// instance i start at node_off[i] in the x / w / phi / f0 pools.
+struct BatchDev {
+  int count;
+  const int *n;            // nodes (elements + 1)
+  const int *nsteps;       // contour steps
+  const double *ds;        // contour step length
+  const long long *node_off;
+  const double *x;         // node coordinates
+  const double *w;         // field (full nodal vector, wall values unused)
+  double *phi;             // density out
+  double *Q;               // (1/L) int q(x,1) dx out
+  const double *qw;        // 16 quadrature weights per instance: [v] for 2-adic class v of the
+                           // sample index (v = min(ctz(k), 14)), [15] for k = 0 and k = nsteps
+  const int *active;       // nonzero: evaluate this instance
+  int *status;             // per-instance status bits (SCFT_ST_*)
+};
+
+// One shape class (C nodes per thread, NW warps per instance) of a batch.
+struct ClassDev {
+  const int *items;        // instance ids, most expensive first
+  int count;
+  int *head;               // work-queue counter (reset to 0 before each launch)
+  void *scratch;           // worker slots for the half-contour store
+  long long slot_elems;    // elements per worker slot
+  int workers;             // number of slots
+  int want;                // evaluate instances whose active flag equals this value
+};
+
+// Status bits written by the kernels.
+enum : int {
+  ST_NOT_DOMINANT = 1,     // system matrix lost diagonal dominance (1 + ds w < 0 somewhere)
+  ST_NONFINITE = 2,        // non-finite density
+  ST_CONVERGED = 4,
+  ST_MAXIT = 8,
+  ST_RESTARTED = 16,
+  ST_WATCHDOG = 32,
+};
+
+}  // namespace scft

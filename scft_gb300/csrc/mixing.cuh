@@ -1,0 +1,65 @@
+// mixing.cuh -- field-update kernels (FP64): batched Anderson mixing and the
+// single-instance reference-form solvers used by the drop-in entry points.
+#pragma once
+#include "common.cuh"
+
+namespace scft {
+
+// Batched Anderson state.  Interior unknowns of instance i start at int_off[i];
+// history slot s of instance i starts at depth*int_off[i] + s*N_i.
+struct MixDev {
+  int count;
+  const int *n;
+  const long long *node_off;
+  const long long *int_off;
+  const double *x, *f0, *phi;
+  double *w;
+  int *active;     // 1: evaluate in FP32, 2: evaluate in FP64, 0: finished
+  int *status;
+  int *iters;
+  double *err;     // ||phi - f0||_inf of the last evaluation
+  double *best;    // best error since the last restart
+  double *graw, *gcur, *gprev, *wprev;  // interior vectors
+  double *hdx, *hdg;                    // history of field / residual differences
+  double *gram;                         // depth*depth per instance
+  int *hcount, *hhead;
+  int depth;
+  int maxit;
+  int mode;        // 0: mixing residual phi - f0; 1: ln phi - ln f0
+  int verify64;    // FP32-converged instances are re-evaluated once in FP64
+  double tol, tol32, beta, clip, grow, precond, reg;
+};
+
+cudaError_t mix_launch(const MixDev &m, cudaStream_t st);
+
+// Single-instance Anderson in the residual form of ADM_chen_C.c:18-147.
+struct AdmChenDev {
+  int n, nm, depth;
+  double *X, *Y;     // depth rows of n (ring by iteration index)
+  double tol, lmd;
+  int final_;
+  // state (device)
+  int *k, *krestart;
+  double *lk, *err;
+  int *flag;         // 0 continue, 1 converged, 2 NaN
+};
+cudaError_t admchen_step_launch(const AdmChenDev &a, cudaStream_t st);
+
+// Single-instance Anderson in the fixed-point ring form of adm.c:24-313.
+struct AdmDev {
+  int n;
+  double *x, *xnew;  // current iterate and g(x)
+  double *xh, *dh;   // 11 slots of n
+  double tol;
+  int *its, *nc;
+  double *err;
+  int *flag;         // 0 continue, 1 converged
+};
+cudaError_t adm_first_launch(const AdmDev &a, cudaStream_t st);
+cudaError_t adm_step_launch(const AdmDev &a, cudaStream_t st);
+
+// residual helpers for the drop-in path
+cudaError_t residual_launch(int n, const double *phi, const double *f0, int sign, double *out_int,
+                            double *w_int_in, int fixed_point, cudaStream_t st);
+
+}  // namespace scft

@@ -1,0 +1,494 @@
+// propagate.cuh -- batched FEM contour propagator + density (the hot path).
+//
+// One "group" of T = 32*NW threads owns one instance at a time; each thread owns
+// C consecutive interior unknowns (a chunk).  Per field iterate the group
+// assembles, in FP64, the implicit-Euler system D = M + ds(K + W) of
+// 1D_FEM.c:95-186 (nonuniform mesh as Matlab_files/simple_FEM_1D_transient.m:34-85)
+// and factors it once for the partition below; then it runs the nsteps contour
+// steps of 1D_FEM.c:208-228 entirely on chip:
+//
+//   chunk level : Thomas sweep over the C-1 chunk-interior unknowns (registers),
+//                 the last unknown of every chunk is its separator;
+//   warp level  : the 32 chunk separators of a warp form a tridiagonal system,
+//                 lanes 0..30 are solved by parallel cyclic reduction with warp
+//                 shuffles, lane 31 is the warp separator;
+//   group level : the NW warp separators form a tridiagonal system solved
+//                 redundantly by every warp (PCR with shuffles); two named
+//                 barriers per step exchange the warp-boundary values.
+//
+// The density phi_i = sum_k W_k q_k,i q_{nsteps-k},i (romint.c:21-57 Romberg
+// weights, or the trapezoid of simple_FEM_1D_transient.m:119-124) is accumulated
+// on the fly: slices k <= nsteps/2 are streamed coalesced to HBM, slices of the
+// second half are multiplied against them as they are produced.
+//
+// FP32 path (DELTA = true): each step solves D dq = -ds (K+W) q for the small
+// increment and adds it to q kept as an unevaluated float pair (hi + lo), so the
+// per-step rounding scales with |dq| instead of |q|.  K q is formed from node
+// differences of the pair, so it is exact on constants: FP32-rounded stiffness
+// bands would not cancel and would bias every step by O(eps ds/h^2).  phi is
+// Kahan-compensated.
+// FP64 path (DELTA = false): the direct form D q' = M q of the reference.
+#pragma once
+#include "common.cuh"
+
+namespace scft {
+
+template <typename R>
+__device__ __forceinline__ R fmaR(R a, R b, R c);
+template <>
+__device__ __forceinline__ float fmaR<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <>
+__device__ __forceinline__ double fmaR<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// hi + lo += d, exact sum of hi and d (Knuth two-sum) folded into lo, then renormalised.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
+  float s = __fadd_rn(hi, d);
+  float bp = __fsub_rn(s, hi);
+  float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(d, bp));
+  float l = __fadd_rn(lo, e);
+  float h = __fadd_rn(s, l);
+  lo = __fsub_rn(l, __fsub_rn(h, s));
+  hi = h;
+}
+
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+template <typename R, int NW>
+struct GroupSmem {
+  R pub_zc0[NW];  // per step, lane 0 of each warp: chunk-local z at its first unknown
+  R pub_zw[NW];   // per step, lane 0 of each warp: warp-level interior solution
+  R pub_R[NW];    // per step, lane 31 of each warp: level-2 right-hand side
+  double s_vc0[NW], s_wc0[NW], s_vw0[NW], s_ww0[NW];
+  double s_A[NW], s_B[NW], s_C[NW];
+  double red[NW];
+  int ired[NW];
+  R qw[16];
+  int item;
+};
+
+template <int NW>
+struct Log2 { static constexpr int v = NW <= 1 ? 0 : 1 + Log2<NW / 2>::v; };
+template <>
+struct Log2<1> { static constexpr int v = 0; };
+
+template <typename R, int C, int NW, bool DELTA>
+struct Propagator {
+  static constexpr int T = 32 * NW;
+  static constexpr int TC = T * C;
+  static constexpr int GPC = (T >= 256) ? 1 : 256 / T;  // groups per CTA
+  static constexpr int CTA = T * GPC;
+  static constexpr int L2 = Log2<NW>::v;
+  static constexpr int CI = (C > 1) ? C - 1 : 1;       // chunk-interior array extent
+
+  __device__ static void gsync(int bar_id) {
+    if (NW > 1) group_sync(bar_id, T);
+    else __syncwarp();
+  }
+
+  __device__ static void run(const BatchDev &b, const ClassDev &cls, GroupSmem<R, NW> &S,
+                             int P, int worker, int bar_id) {
+    const int lane = P & 31, wid = P >> 5;
+    R *slot = reinterpret_cast<R *>(cls.scratch) + (long long)worker * cls.slot_elems;
+    for (;;) {
+      int item;
+      if (NW > 1) {
+        if (P == 0) S.item = atomicAdd(cls.head, 1);
+        gsync(bar_id);
+        item = S.item;
+        gsync(bar_id);
+      } else {
+        item = 0;
+        if (lane == 0) item = atomicAdd(cls.head, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+      }
+      if (item >= cls.count) break;
+      const int inst = cls.items[item];
+      if (b.active[inst] != cls.want) continue;
+      instance(b, S, P, lane, wid, inst, slot, bar_id);
+    }
+  }
+
+  __device__ static void instance(const BatchDev &b, GroupSmem<R, NW> &S, int P, int lane, int wid,
+                                  int inst, R *slot, int bar_id) {
+    const unsigned FULL = 0xffffffffu;
+    const int n = b.n[inst], N = n - 2, ns = b.nsteps[inst], half = ns / 2;
+    const double ds = b.ds[inst];
+    const long long off = b.node_off[inst];
+    const double *x = b.x + off;
+    const double *w = b.w + off;
+    if (P < 16) S.qw[P] = (R)b.qw[(long long)inst * 16 + P];
+    gsync(bar_id);
+    int bad = 0;
+
+    // ---------------- setup (FP64): bands, chunk LU, spikes ----------------
+    // Right-hand side bands.  Direct form: the mass matrix.  Increment form:
+    // -ds (K + W) q with the stiffness applied to node differences (ka, kb =
+    // ds/a1, ds/a2) so that it vanishes exactly on constants in FP32, and the
+    // field term -ds w M in (cl, cd, cu).
+    double dl[C], dd[C], du[C];
+    R cl[C], cd[C], cu[C], ka[C], kb[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const int j = P * C + c;
+      ka[c] = kb[c] = (R)0;
+      if (j < N) {
+        const int i = j + 1;
+        const double a1 = x[i] - x[i - 1], a2 = x[i + 1] - x[i];
+        const double ml = a1 / 6.0, md = a1 / 3.0 + a2 / 3.0, mu = a2 / 6.0;
+        const double kl = -1.0 / a1, kd = 1.0 / a1 + 1.0 / a2, ku = -1.0 / a2;
+        const double wi = w[i];
+        const double al = kl + wi * ml, ad = kd + wi * md, au = ku + wi * mu;
+        dl[c] = (j == 0) ? 0.0 : ml + ds * al;
+        dd[c] = md + ds * ad;
+        du[c] = (j == N - 1) ? 0.0 : mu + ds * au;
+        if constexpr (DELTA) {
+          ka[c] = (R)(ds / a1);
+          kb[c] = (R)(ds / a2);
+          cl[c] = (R)((j == 0) ? 0.0 : -ds * wi * ml);
+          cd[c] = (R)(-ds * wi * md);
+          cu[c] = (R)((j == N - 1) ? 0.0 : -ds * wi * mu);
+        } else {
+          cl[c] = (R)((j == 0) ? 0.0 : ml);
+          cd[c] = (R)md;
+          cu[c] = (R)((j == N - 1) ? 0.0 : mu);
+        }
+        if (!(dd[c] > fabs(dl[c]) + fabs(du[c]))) bad |= ST_NOT_DOMINANT;
+      } else {
+        dl[c] = 0.0; dd[c] = 1.0; du[c] = 0.0;
+        cl[c] = cd[c] = cu[c] = (R)0;
+      }
+    }
+    // chunk-interior LU (unknowns 0..C-2) and spikes
+    R mm[CI], ib[CI], ub[CI], vc[CI], wc[CI];
+    double vc0 = 0.0, wc0 = 0.0, vcl = 0.0, wcl = 0.0;  // spikes at interior index 0 and C-2
+    if (C > 1) {
+      double ibd[CI], ubd[CI], mmd[CI], v[CI], ww[CI];
+      double beta = dd[0];
+      ibd[0] = 1.0 / beta; ubd[0] = du[0] * ibd[0]; mmd[0] = 0.0;
+#pragma unroll
+      for (int k = 1; k < C - 1; k++) {
+        mmd[k] = dl[k] * ibd[k - 1];
+        beta = dd[k] - mmd[k] * du[k - 1];
+        ibd[k] = 1.0 / beta;
+        ubd[k] = du[k] * ibd[k];
+      }
+      // v = D_II^{-1} (dl[0] e_0),  w = D_II^{-1} (du[C-2] e_{C-2})
+      v[0] = dl[0];
+#pragma unroll
+      for (int k = 1; k < C - 1; k++) v[k] = -mmd[k] * v[k - 1];
+      v[C - 2] *= ibd[C - 2];
+#pragma unroll
+      for (int k = C - 3; k >= 0; k--) v[k] = v[k] * ibd[k] - ubd[k] * v[k + 1];
+      ww[C - 2] = du[C - 2] * ibd[C - 2];
+#pragma unroll
+      for (int k = C - 3; k >= 0; k--) ww[k] = -ubd[k] * ww[k + 1];
+#pragma unroll
+      for (int k = 0; k < C - 1; k++) {
+        mm[k] = (R)mmd[k]; ib[k] = (R)ibd[k]; ub[k] = (R)ubd[k];
+        vc[k] = (R)v[k]; wc[k] = (R)ww[k];
+      }
+      vc0 = v[0]; wc0 = ww[0]; vcl = v[C - 2]; wcl = ww[C - 2];
+    } else {
+#pragma unroll
+      for (int k = 0; k < CI; k++) mm[k] = ib[k] = ub[k] = vc[k] = wc[k] = (R)0;
+    }
+    // next chunk's spikes at its first interior unknown (lane 31: from the next warp)
+    double vcn = __shfl_down_sync(FULL, vc0, 1), wcn = __shfl_down_sync(FULL, wc0, 1);
+    if (NW > 1) {
+      if (lane == 0) { S.s_vc0[wid] = vc0; S.s_wc0[wid] = wc0; }
+      gsync(bar_id);
+      if (lane == 31) {
+        vcn = (wid + 1 < NW) ? S.s_vc0[wid + 1] : 0.0;
+        wcn = (wid + 1 < NW) ? S.s_wc0[wid + 1] : 0.0;
+      }
+    } else if (lane == 31) {
+      vcn = 0.0; wcn = 0.0;
+    }
+    // chunk-separator system: al_p S_{p-1} + be_p S_p + ga_p S_{p+1} = rho_p
+    const double dls = dl[C - 1], dds = dd[C - 1], dus = du[C - 1];
+    double al, be, ga;
+    if (C > 1) {
+      al = -dls * vcl;
+      be = dds - dls * wcl - dus * vcn;
+      ga = -dus * wcn;
+    } else {
+      al = dls; be = dds; ga = dus;
+    }
+    // warp level: lanes 0..30 interior (couplings of lane 0 to the previous warp
+    // separator and of lane 30 to lane 31 moved into spikes), lane 31 identity
+    R K1[5], K2[5];
+    R ibw;
+    double vw, ww;
+    {
+      double a = (lane == 0 || lane == 31) ? 0.0 : al;
+      double bb = (lane == 31) ? 1.0 : be;
+      double c = (lane >= 30) ? 0.0 : ga;
+      double k1d[5], k2d[5];
+#pragma unroll
+      for (int l = 0; l < 5; l++) {
+        const int s = 1 << l;
+        const double am = __shfl_up_sync(FULL, a, s), bm = __shfl_up_sync(FULL, bb, s),
+                     cm = __shfl_up_sync(FULL, c, s);
+        const double ap = __shfl_down_sync(FULL, a, s), bp = __shfl_down_sync(FULL, bb, s),
+                     cp = __shfl_down_sync(FULL, c, s);
+        const double k1 = (lane >= s) ? a / bm : 0.0;
+        const double k2 = (lane + s < 32) ? c / bp : 0.0;
+        const double na = -k1 * am, nc = -k2 * cp, nb = bb - k1 * cm - k2 * ap;
+        a = na; c = nc; bb = nb;
+        k1d[l] = k1; k2d[l] = k2;
+        K1[l] = (R)k1; K2[l] = (R)k2;
+      }
+      const double ibwd = 1.0 / bb;
+      ibw = (R)ibwd;
+      // spikes of the warp interior system
+      double rv = (lane == 0) ? al : 0.0, rw = (lane == 30) ? ga : 0.0;
+#pragma unroll
+      for (int l = 0; l < 5; l++) {
+        const int s = 1 << l;
+        const double vm = __shfl_up_sync(FULL, rv, s), vp = __shfl_down_sync(FULL, rv, s);
+        const double wm = __shfl_up_sync(FULL, rw, s), wp = __shfl_down_sync(FULL, rw, s);
+        rv = rv - k1d[l] * vm - k2d[l] * vp;
+        rw = rw - k1d[l] * wm - k2d[l] * wp;
+      }
+      vw = (lane == 31) ? 0.0 : rv * ibwd;
+      ww = (lane == 31) ? 0.0 : rw * ibwd;
+    }
+    // level 2: warp separators
+    const double vw30 = __shfl_sync(FULL, vw, 30), ww30 = __shfl_sync(FULL, ww, 30);
+    double vwn = 0.0, wwn = 0.0;
+    R K1b[L2 > 0 ? L2 : 1], K2b[L2 > 0 ? L2 : 1];
+    R iB2;
+    if (NW > 1) {
+      if (lane == 0) { S.s_vw0[wid] = vw; S.s_ww0[wid] = ww; }
+      gsync(bar_id);
+      if (lane == 31) {
+        vwn = (wid + 1 < NW) ? S.s_vw0[wid + 1] : 0.0;
+        wwn = (wid + 1 < NW) ? S.s_ww0[wid + 1] : 0.0;
+        S.s_A[wid] = (wid == 0) ? 0.0 : -al * vw30;
+        S.s_B[wid] = be - al * ww30 - ga * vwn;
+        S.s_C[wid] = (wid + 1 < NW) ? -ga * wwn : 0.0;
+      }
+      gsync(bar_id);
+      double a = (lane < NW) ? S.s_A[lane] : 0.0;
+      double bb = (lane < NW) ? S.s_B[lane] : 1.0;
+      double c = (lane < NW) ? S.s_C[lane] : 0.0;
+#pragma unroll
+      for (int l = 0; l < L2; l++) {
+        const int s = 1 << l;
+        const double am = __shfl_up_sync(FULL, a, s), bm = __shfl_up_sync(FULL, bb, s),
+                     cm = __shfl_up_sync(FULL, c, s);
+        const double ap = __shfl_down_sync(FULL, a, s), bp = __shfl_down_sync(FULL, bb, s),
+                     cp = __shfl_down_sync(FULL, c, s);
+        const double k1 = (lane >= s) ? a / bm : 0.0;
+        const double k2 = (lane + s < NW) ? c / bp : 0.0;
+        const double na = -k1 * am, nc = -k2 * cp, nb = bb - k1 * cm - k2 * ap;
+        a = na; c = nc; bb = nb;
+        K1b[l] = (R)k1; K2b[l] = (R)k2;
+      }
+      iB2 = (R)(1.0 / bb);
+    } else {
+      K1b[0] = K2b[0] = (R)0;
+      iB2 = (R)(1.0 / (be - al * ww30));  // meaningful in lane 31
+    }
+    const R r_al = (R)al, r_ga = (R)ga, r_vw = (R)vw, r_ww = (R)ww, r_vwn = (R)vwn, r_wwn = (R)wwn;
+    const R r_dls = (R)dls, r_dus = (R)dus, r_vcn = (R)vcn, r_wcn = (R)wcn;
+    const bool last_chunk = (P == T - 1);
+
+    // ---------------- state ----------------
+    R qh[C], ql[C], acc[C], cmp[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const int j = P * C + c;
+      qh[c] = (j < N) ? (R)1 : (R)0;
+      ql[c] = (R)0; acc[c] = (R)0; cmp[c] = (R)0;
+    }
+    R qLh = (P * C - 1 >= 0 && P * C - 1 < N) ? (R)1 : (R)0, qLl = (R)0;
+    R qRh = ((P + 1) * C < N) ? (R)1 : (R)0, qRl = (R)0;
+#pragma unroll
+    for (int c = 0; c < C; c++) slot[(long long)c * T + P] = qh[c];
+    const R wend = S.qw[15];
+
+    // ---------------- contour loop ----------------
+    for (int k = 1; k <= ns; k++) {
+      const bool acc_step = (k >= ns - half);
+      const bool self_pair = (k == ns - k);
+      R pre[C];
+      if (acc_step && !self_pair) {
+        const R *src = slot + (long long)(ns - k) * TC + P;
+#pragma unroll
+        for (int c = 0; c < C; c++) pre[c] = src[(long long)c * T];
+      }
+      // right-hand side
+      R r[C];
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const R left = (c == 0) ? qLh : qh[c - 1];
+        const R right = (c == C - 1) ? qRh : qh[c + 1];
+        r[c] = fmaR(cu[c], right, fmaR(cl[c], left, cd[c] * qh[c]));
+        if constexpr (DELTA) {
+          const R leftl = (c == 0) ? qLl : ql[c - 1];
+          const R rightl = (c == C - 1) ? qRl : ql[c + 1];
+          const R d1 = (qh[c] - left) + (ql[c] - leftl);
+          const R d2 = (qh[c] - right) + (ql[c] - rightl);
+          r[c] -= fmaR(ka[c], d1, kb[c] * d2);
+        }
+      }
+      // chunk-interior Thomas sweep
+      R zc[CI];
+      if (C > 1) {
+        R y = r[0];
+        zc[0] = y;
+#pragma unroll
+        for (int kk = 1; kk < C - 1; kk++) { y = fmaR(-mm[kk], y, r[kk]); zc[kk] = y; }
+        zc[C - 2] = zc[C - 2] * ib[C - 2];
+#pragma unroll
+        for (int kk = C - 3; kk >= 0; kk--) zc[kk] = fmaR(-ub[kk], zc[kk + 1], zc[kk] * ib[kk]);
+      } else {
+        zc[0] = (R)0;
+      }
+      R zc0n = __shfl_down_sync(FULL, zc[0], 1);
+      // chunk-separator right-hand side and warp-interior PCR
+      R rho = (C > 1) ? fmaR(-r_dus, zc0n, fmaR(-r_dls, zc[C > 1 ? C - 2 : 0], r[C - 1])) : r[0];
+      R t = (lane == 31) ? (R)0 : rho;
+#pragma unroll
+      for (int l = 0; l < 5; l++) {
+        const int s = 1 << l;
+        const R tm = __shfl_up_sync(FULL, t, s), tp = __shfl_down_sync(FULL, t, s);
+        t = fmaR(-K2[l], tp, fmaR(-K1[l], tm, t));
+      }
+      const R zw = t * ibw;
+      const R zw30 = __shfl_sync(FULL, zw, 30);
+      R Sprevw, Sown, Snextw, zwn = (R)0;
+      if (NW > 1) {
+        if (lane == 0) { S.pub_zc0[wid] = zc[0]; S.pub_zw[wid] = zw; }
+        gsync(bar_id);
+        if (lane == 31) {
+          const bool has_next = (wid + 1 < NW);
+          const R zcx = has_next ? S.pub_zc0[wid + 1] : (R)0;
+          zwn = has_next ? S.pub_zw[wid + 1] : (R)0;
+          if (C > 1) {
+            zc0n = zcx;
+            rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zc[C > 1 ? C - 2 : 0], r[C - 1]));
+          }
+          S.pub_R[wid] = fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho));
+        }
+        gsync(bar_id);
+        R t2 = (lane < NW) ? S.pub_R[lane] : (R)0;
+#pragma unroll
+        for (int l = 0; l < L2; l++) {
+          const int s = 1 << l;
+          const R tm = __shfl_up_sync(FULL, t2, s), tp = __shfl_down_sync(FULL, t2, s);
+          t2 = fmaR(-K2b[l], tp, fmaR(-K1b[l], tm, t2));
+        }
+        const R sw = t2 * iB2;
+        Sown = __shfl_sync(FULL, sw, wid);
+        Sprevw = __shfl_sync(FULL, sw, wid > 0 ? wid - 1 : 0);
+        Snextw = __shfl_sync(FULL, sw, wid + 1 < NW ? wid + 1 : wid);
+        if (wid == 0) Sprevw = (R)0;
+        if (wid + 1 >= NW) Snextw = (R)0;
+      } else {
+        const R Rw = fmaR(-r_al, zw30, rho);
+        Sown = __shfl_sync(FULL, Rw * iB2, 31);
+        Sprevw = (R)0;
+        Snextw = (R)0;
+      }
+      // separator values and their neighbours
+      const R Sp = (lane == 31) ? Sown : fmaR(-r_ww, Sown, fmaR(-r_vw, Sprevw, zw));
+      R Sprev = __shfl_up_sync(FULL, Sp, 1);
+      R Snext = __shfl_down_sync(FULL, Sp, 1);
+      if (lane == 0) Sprev = Sprevw;
+      if (lane == 31) Snext = (NW > 1 && wid + 1 < NW) ? fmaR(-r_wwn, Snextw, fmaR(-r_vwn, Sown, zwn)) : (R)0;
+      // chunk unknowns
+      R xv[C];
+#pragma unroll
+      for (int c = 0; c < C - 1; c++) xv[c] = fmaR(-wc[c], Sp, fmaR(-vc[c], Sprev, zc[c]));
+      xv[C - 1] = Sp;
+      const R dL = Sprev;
+      R dR = (C > 1) ? fmaR(-r_wcn, Snext, fmaR(-r_vcn, Sp, zc0n)) : Snext;
+      if (last_chunk) dR = (R)0;
+      if constexpr (DELTA) {
+#pragma unroll
+        for (int c = 0; c < C; c++) ff_add(qh[c], ql[c], xv[c]);
+        ff_add(qLh, qLl, dL);
+        ff_add(qRh, qRl, dR);
+      } else {
+#pragma unroll
+        for (int c = 0; c < C; c++) qh[c] = xv[c];
+        qLh = dL;
+        qRh = dR;
+      }
+      // half-contour store / density accumulation
+      if (k <= half) {
+        R *dst = slot + (long long)k * TC + P;
+#pragma unroll
+        for (int c = 0; c < C; c++) dst[(long long)c * T] = qh[c];
+      }
+      if (acc_step) {
+        R wk = (k == ns) ? wend : S.qw[min(__ffs(k) - 1, 14)];
+        if (!self_pair) wk = wk + wk;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          const R other = self_pair ? qh[c] : pre[c];
+          const R term = (wk * qh[c]) * other;
+          if constexpr (DELTA) {
+            const R y = term - cmp[c];
+            const R tt = acc[c] + y;
+            cmp[c] = (tt - acc[c]) - y;
+            acc[c] = tt;
+          } else {
+            acc[c] += term;
+          }
+        }
+      }
+    }
+
+    // ---------------- epilogue: phi, Q, status ----------------
+    double qpart = 0.0;
+    double *phi = b.phi + off;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const int j = P * C + c;
+      if (j < N) {
+        const double v = (double)acc[c] - (double)cmp[c];
+        if (!isfinite(v)) bad |= ST_NONFINITE;
+        phi[j + 1] = v;
+        qpart += 0.5 * (x[j + 2] - x[j]) * ((double)qh[c] + (double)ql[c]);
+      }
+    }
+    if (P == 0) { phi[0] = 0.0; phi[n - 1] = 0.0; }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      qpart += __shfl_down_sync(FULL, qpart, s);
+      bad |= __shfl_down_sync(FULL, bad, s);
+    }
+    if (NW > 1) {
+      if (lane == 0) { S.red[wid] = qpart; S.ired[wid] = bad; }
+      gsync(bar_id);
+      if (P == 0) {
+        qpart = 0.0;
+        for (int q = 0; q < NW; q++) { qpart += S.red[q]; bad |= S.ired[q]; }
+      }
+      gsync(bar_id);
+    }
+    if (P == 0) {
+      b.Q[inst] = qpart / (x[n - 1] - x[0]);
+      if (bad) atomicOr(&b.status[inst], bad);
+    }
+  }
+};
+
+template <typename R, int C, int NW, bool DELTA>
+__global__ void __launch_bounds__(Propagator<R, C, NW, DELTA>::CTA)
+propagate_kernel(BatchDev b, ClassDev cls) {
+  using Pp = Propagator<R, C, NW, DELTA>;
+  __shared__ GroupSmem<R, NW> sm[Pp::GPC];
+  const int g = threadIdx.x / Pp::T;
+  const int P = threadIdx.x % Pp::T;
+  const int worker = blockIdx.x * Pp::GPC + g;
+  if (worker >= cls.workers) return;
+  Pp::run(b, cls, sm[g], P, worker, 1 + g);
+}
+
+}  // namespace scft

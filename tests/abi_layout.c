@@ -1,0 +1,26 @@
+/* Prints the size and field offsets of the C ABI structs of include/scft.h, one
+   per line, so that tests/test_abi.py can check the ctypes mirror against the
+   compiler's layout. */
+#include <stddef.h>
+#include <stdio.h>
+
+#include "scft.h"
+
+#define F(T, m) printf(#T "." #m " %zu\n", offsetof(T, m))
+int main(void) {
+  printf("scft_config %zu\n", sizeof(scft_config));
+  F(scft_config, n_nodes); F(scft_config, x); F(scft_config, L); F(scft_config, f0);
+  F(scft_config, nsteps); F(scft_config, ds); F(scft_config, rule); F(scft_config, sign);
+  F(scft_config, precision);
+  printf("scft_instance %zu\n", sizeof(scft_instance));
+  F(scft_instance, n_nodes); F(scft_instance, x); F(scft_instance, L); F(scft_instance, f0);
+  F(scft_instance, w0); F(scft_instance, nsteps); F(scft_instance, ds); F(scft_instance, rule);
+  printf("scft_solve_opts %zu\n", sizeof(scft_solve_opts));
+  F(scft_solve_opts, precision); F(scft_solve_opts, tol); F(scft_solve_opts, tol32_factor);
+  F(scft_solve_opts, verify64); F(scft_solve_opts, maxit); F(scft_solve_opts, depth);
+  F(scft_solve_opts, beta); F(scft_solve_opts, clip); F(scft_solve_opts, grow); F(scft_solve_opts, reg);
+  F(scft_solve_opts, residual_mode); F(scft_solve_opts, precond); F(scft_solve_opts, iters_per_graph);
+  printf("scft_result %zu\n", sizeof(scft_result));
+  F(scft_result, status); F(scft_result, iterations); F(scft_result, err); F(scft_result, Q);
+  return 0;
+}

@@ -1,0 +1,122 @@
+"""GPU field updates: the reference solvers' entry points (adm, adm_chen, broydn)
+against the reference's outputs, and the batched solver against the oracle."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from scft_gb300 import F32, F64, RULE_ROMBERG, RULE_TRAPEZOID, ST_CONVERGED, api, workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return json.load(open(os.path.join(GOLD, name)))
+
+
+def toy3(v):
+    x, y, z = v
+    return np.array([x * y * z - 12.0, x * x + y * y - 8.0, x + y + z - 511.0])
+
+
+def test_adm_chen_toy_matches_reference():
+    c = load("nr_routines.json")["adm_chen_toy"]
+    rc, x = api.adm_chen(toy3, c["x0"], c["tol"], c["maxit"], 3, c["lmd"], c["nn"])
+    assert rc == c["rc"] == 0
+    np.testing.assert_allclose(x, c["x"], rtol=1e-9)
+
+
+def test_adm_toy_matches_reference():
+    c = load("nr_routines.json")["adm_toy"]
+    myfun = lambda v: np.array([0.5 * v[0] - 2.0, 0.5 * v[1] + 3.0])  # noqa: E731
+    for flag in (0, 1):
+        x, chk = api.adm(c["x0"], 2, myfun, flag=flag, maxit=1000)
+        assert chk == c["check"] == 0
+        np.testing.assert_allclose(x, c["x"], rtol=1e-10)
+
+
+def test_broydn_toy_matches_reference():
+    c = load("nr_routines.json")["broydn_toy"]
+    x, chk, err = api.broydn(c["x0"], 3, toy3, c["tol"])
+    np.testing.assert_allclose(x, c["x"], rtol=1e-7)
+
+
+def matlab_problem():
+    g = load("matlab_N33.json")
+    api.set_config(np.array(g["f0"]), x=np.array(g["x"]), nsteps=2049, ds=1.0 / 2048,
+                   rule=RULE_TRAPEZOID, sign=-1)
+    return g
+
+
+def test_adm_chen_scft_first_iterates_on_device():
+    """GPU adm_chen with the on-device propagator follows the reference
+    adm_chen's first iterates (reference driving the oracle propagator).  Later
+    iterates drift apart at the rate the ill-conditioned least-squares system
+    amplifies 1e-16 rounding differences, so the step itself is checked by
+    replay below."""
+    matlab_problem()
+    s = load("admchen_scft.json")
+    traj = np.array(s["trajectory"])
+    for k in (0, 1, 2, 3):
+        rc, x = api.adm_chen(api.FEM_RESIDUAL0, s["w0"], s["tol"], k, len(s["w0"]), s["lmd"], s["nn"])
+        np.testing.assert_allclose(x, traj[k + 1], rtol=0, atol=1e-8 * np.abs(traj).max())
+
+
+def test_adm_chen_step_replays_reference():
+    """Replaying the reference's recorded residuals (call by call), the GPU
+    adm_chen update reproduces every reference iterate."""
+    s = load("admchen_scft.json")
+    traj, ys = np.array(s["trajectory"]), np.array(s["residuals"])
+    calls = []
+
+    def replay(x):
+        calls.append(x.copy())
+        return ys[len(calls) - 1]
+
+    rc, x = api.adm_chen(replay, s["w0"], s["tol"], len(ys) - 1, len(s["w0"]), s["lmd"], s["nn"])
+    got = np.array(calls)
+    np.testing.assert_allclose(got, traj[:len(got)], rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(x, s["x_final"], rtol=1e-10, atol=1e-10)
+
+
+def test_broydn_scft_matches_reference():
+    matlab_problem()
+    s = load("broydn_scft.json")
+    x, chk, err = api.broydn(s["w0"], len(s["w0"]), api.FEM_RESIDUAL, s["tol"])
+    assert chk == 0 and err < s["tol"]
+    np.testing.assert_allclose(x, s["x"], rtol=1e-6, atol=1e-8)
+
+
+def test_adm_fixed_point_form_on_device():
+    g = matlab_problem()
+    w0 = np.array(g["w"])[1:-1] + 0.01
+    x, chk = api.adm(w0, len(w0), api.FEM_FIXEDPOINT, flag=1, maxit=40)
+    r = api.fem_residual(x)
+    assert np.abs(r).max() < np.abs(api.fem_residual(w0)).max()
+
+
+def oracle_residual(O, d, w):
+    p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d.get("rule", RULE_ROMBERG))
+    return O.residual(p, w[1:-1])[0]
+
+
+def test_batch_solve_single_small_fp64(oracle):
+    d = W.single_small()
+    with api.Batch([d]) as b:
+        r = b.solve(precision=F64, tol=1e-8, maxit=2000)
+        w, phi, Q = b.get()
+    assert r["status"][0] & ST_CONVERGED
+    assert np.abs(oracle_residual(oracle, d, w[0])).max() <= 1e-8 * (1 + 1e-6)
+
+
+def test_batch_solve_mixed_fp32(oracle):
+    insts = W.batch_mixed(24, seed=21)
+    with api.Batch(insts) as b:
+        r = b.solve(precision=F32, tol=1e-6, maxit=3000)
+        w, phi, Q = b.get()
+    assert np.all(r["status"] & ST_CONVERGED), r
+    for i, d in enumerate(insts):
+        assert np.abs(oracle_residual(oracle, d, w[i])).max() <= 1e-6, i
