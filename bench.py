@@ -158,21 +158,6 @@ def make_workload(name: str, count: int | None):
     raise SystemExit(f"unknown workload {name}")
 
 
-def shard(instances, rank, world):
-    """Cost-balanced (longest-first greedy) split of the batch across ranks."""
-    if world == 1:
-        return list(range(len(instances)))
-    cost = [(d["n_nodes"] * d["nsteps"], i) for i, d in enumerate(instances)]
-    cost.sort(reverse=True)
-    load = [0.0] * world
-    parts = [[] for _ in range(world)]
-    for c, i in cost:
-        r = min(range(world), key=lambda k: load[k])
-        load[r] += c
-        parts[r].append(i)
-    return sorted(parts[rank])
-
-
 def instance_bytes(insts):
     h2d = 0
     d2h = 0
@@ -262,6 +247,7 @@ def reference_arm(args):
 def ours_arm(args):
     rank, world, local, torch = dist_setup(want_gpu=True)
     from scft_gb300 import F32, F64, ST_CONVERGED, api
+    from scft_gb300.shard import shard
 
     insts, desc = make_workload(args.workload, args.count)
     mine = [insts[i] for i in shard(insts, rank, world)]

@@ -183,6 +183,44 @@ int scft_batch_set_shape(scft_batch *b, int precision, int index, int C, int NW)
 int scft_batch_autotune(scft_batch *b, int precision);
 int scft_batch_destroy(scft_batch *b);
 
+/* =========================================================================
+ * Learned warm start.  No counterpart in the reference, which reads its
+ * initial fields from files (1D_FEM.c:321-342, DEALII_SCFT/src/scft_util.cc:14-41).
+ * A 1D-conv network (4 dilated layers, 64 channels, kernel 5, FP32 weights,
+ * BF16 activations) maps the film width L, the contour step count and the
+ * target profile on a 256-point grid of the mesh coordinate to w0(x).  The
+ * plain mixing loop still converges every instance to the same tolerance.
+ * ========================================================================= */
+
+typedef struct scft_ws scft_ws;
+
+/* act_bf16 = 1 stores hidden activations in BF16 (0: FP32, for gradient checks). */
+int scft_ws_create(int act_bf16, unsigned long long seed, scft_ws **out);
+int scft_ws_destroy(scft_ws *ws);
+/* Number of FP32 parameters (weights then bias of each layer), or an error code. */
+int scft_ws_param_count(scft_ws *ws);
+int scft_ws_get_params(scft_ws *ws, float *out);
+int scft_ws_set_params(scft_ws *ws, const float *in);
+/* Host buffers: features B x 4 x 256, out B x 256 (w / 5 on the grid). */
+int scft_ws_forward(scft_ws *ws, const float *features, int B, float *out);
+/* Mean-squared error of the forward pass against targets (B x 256) and its
+   gradient with respect to every parameter (param_count floats). */
+int scft_ws_loss_grad(scft_ws *ws, const float *features, const float *targets, int B, double *loss,
+                      float *grad);
+/* The network inputs of every instance of a batch (count x 4 x 256) and, when
+   targets != NULL, its current fields resampled to the grid (count x 256, / 5). */
+int scft_ws_batch_features(scft_batch *b, float *features, float *targets);
+/* Append the instances of b selected by mask (NULL: all) with their current
+   fields as training samples.  Returns the dataset size or an error code. */
+int scft_ws_dataset_from_batch(scft_ws *ws, scft_batch *b, const int *mask);
+/* Adam on the dataset: steps minibatches of `batch` samples; losses (steps
+   floats, may be NULL) receives the minibatch losses. */
+int scft_ws_train(scft_ws *ws, int steps, int batch, float lr, unsigned long long seed, float *losses);
+/* Overwrite every field of b with the network's prediction (on b's stream;
+   scft_batch_last_ms reports its device time). */
+int scft_ws_predict(scft_ws *ws, scft_batch *b);
+const char *scft_ws_last_error(void);
+
 /* Kernels launched by this library since load (graph replays count each node). */
 long long scft_kernel_launches(void);
 

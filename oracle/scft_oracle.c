@@ -1012,18 +1012,13 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
     if (bad) { rc = 2; break; }
     if (e <= o->tol) { rc = 0; break; }
     if (it >= o->maxit) { rc = 1; break; }
-    for (int j = 0; j < N; j++) {
-      double gc = graw[j], gm = j > 0 ? graw[j - 1] : 0.0, gp = j < N - 1 ? graw[j + 1] : 0.0;
-      double a1 = p->x[j + 1] - p->x[j], a2 = p->x[j + 2] - p->x[j + 1];
-      g[j] = gc + o->precond * ((gc - gm) / a1 + (gc - gp) / a2) / (0.5 * (a1 + a2));
-    }
     int restart = (it > 0) && (e > o->grow * best);
     if (restart) { cnt = 0; best = e; }
     else best = (it == 0) ? e : fmin(best, e);
     int push = (it > 0) && !restart, h = head;
     if (push) {
       for (int j = 0; j < N; j++) {
-        hdg[(size_t)h * N + j] = g[j] - gprev[j];
+        hdg[(size_t)h * N + j] = graw[j] - gprev[j];
         hdx[(size_t)h * N + j] = w[j + 1] - wprev[j];
       }
       head = (head + 1) % D;
@@ -1037,7 +1032,7 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
         const double *ds_ = hdg + (size_t)slot[t] * N;
         double sb = 0.0, sg = 0.0;
         for (int j = 0; j < N; j++) {
-          sb += ds_[j] * g[j];
+          sb += ds_[j] * graw[j];
           if (push) sg += hdg[(size_t)h * N + j] * ds_[j];
         }
         gam[t] = sb;
@@ -1052,21 +1047,27 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
       for (int t = 0; t < cnt; t++) A[t * cnt + t] += o->reg * dmax + 1e-300;
       small_solve_pp(A, gam, cnt);
     }
+    /* mixed residual, then the preconditioned step */
+    for (int j = 0; j < N; j++) {
+      double rb = graw[j];
+      for (int t = 0; t < cnt; t++) rb -= gam[t] * hdg[(size_t)slot[t] * N + j];
+      g[j] = rb;
+    }
     double dm = 0.0;
     for (int j = 0; j < N; j++) {
-      double d = o->beta * g[j];
-      for (int t = 0; t < cnt; t++) {
-        size_t off = (size_t)slot[t] * N + j;
-        d -= gam[t] * (hdx[off] + o->beta * hdg[off]);
-      }
-      graw[j] = d;
-      dm = fmax(dm, fabs(d));
+      double gc = g[j], gm = j > 0 ? g[j - 1] : 0.0, gp = j < N - 1 ? g[j + 1] : 0.0;
+      double a1 = p->x[j + 1] - p->x[j], a2 = p->x[j + 2] - p->x[j + 1];
+      double step = o->beta * (gc + o->precond * ((gc - gm) / a1 + (gc - gp) / a2) / (0.5 * (a1 + a2)));
+      for (int t = 0; t < cnt; t++) step -= gam[t] * hdx[(size_t)slot[t] * N + j];
+      wprev[j] = step;
+      dm = fmax(dm, fabs(step));
     }
     double scale = dm > o->clip ? o->clip / dm : 1.0;
     for (int j = 0; j < N; j++) {
+      double step = wprev[j];
       wprev[j] = w[j + 1];
-      gprev[j] = g[j];
-      w[j + 1] += scale * graw[j];
+      gprev[j] = graw[j];
+      w[j + 1] += scale * step;
     }
   }
   if (iters) *iters = it;

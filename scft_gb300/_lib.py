@@ -31,6 +31,7 @@ F32, F64 = 0, 1
 MIX_LINEAR, MIX_LOG = 0, 1
 
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 VECFUNC = C.CFUNCTYPE(None, C.c_int, _dp, _dp)
 
 
@@ -89,6 +90,18 @@ SIGNATURES = {
     "scft_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "scft_batch_destroy": (C.c_int, [C.c_void_p]),
     "scft_kernel_launches": (C.c_longlong, []),
+    "scft_ws_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "scft_ws_destroy": (C.c_int, [C.c_void_p]),
+    "scft_ws_param_count": (C.c_int, [C.c_void_p]),
+    "scft_ws_get_params": (C.c_int, [C.c_void_p, _fp]),
+    "scft_ws_set_params": (C.c_int, [C.c_void_p, _fp]),
+    "scft_ws_forward": (C.c_int, [C.c_void_p, _fp, C.c_int, _fp]),
+    "scft_ws_loss_grad": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int, _dp, _fp]),
+    "scft_ws_batch_features": (C.c_int, [C.c_void_p, _fp, _fp]),
+    "scft_ws_dataset_from_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    "scft_ws_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _fp]),
+    "scft_ws_predict": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "scft_ws_last_error": (C.c_char_p, []),
 }
 
 _lib = None
@@ -116,7 +129,8 @@ def load(path: str | None = None):
 class ScftError(RuntimeError):
     def __init__(self, code: int, where: str):
         lib = load()
-        msg = lib.scft_last_error().decode() or lib.scft_strerror(code).decode()
+        msg = (lib.scft_last_error().decode() or lib.scft_ws_last_error().decode()
+               or lib.scft_strerror(code).decode())
         super().__init__(f"{where}: {msg} (code {code})")
         self.code = code
 

@@ -1,9 +1,9 @@
 // mixing.cu -- FP64 field-update kernels.
 //
 // mix_kernel        batched Anderson mixing (one CTA per instance) used by the
-//                   batched solver: residual check, preconditioned mixing
-//                   residual, difference-form history, regularised least squares,
-//                   step clipping and restart safeguards.
+//                   batched solver: residual check, difference-form history of
+//                   the mixing residual, regularised least squares, a
+//                   preconditioned and clipped step, restart safeguard.
 // admchen_step_*    one iteration of ADM_chen_C.c:55-135 for the drop-in solver.
 // adm_*             one iteration of adm.c:103-306 for the drop-in solver.
 #include "mixing.cuh"
@@ -109,16 +109,7 @@ __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
     if (tid == 0) { m.status[inst] |= ST_MAXIT; m.active[inst] = 0; m.err[inst] = e; }
     return;
   }
-  __syncthreads();
-  // 2. preconditioned mixing residual g = (1 + a * (-lap)) graw, lumped FEM Laplacian
-  for (int j = tid; j < N; j += MIX_THREADS) {
-    const double gc = graw[j];
-    const double gm = (j > 0) ? graw[j - 1] : 0.0, gp = (j < N - 1) ? graw[j + 1] : 0.0;
-    const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
-    const double lap = ((gc - gm) / a1 + (gc - gp) / a2) / (0.5 * (a1 + a2));
-    gcur[j] = gc + m.precond * lap;
-  }
-  // 3. history bookkeeping (restart when the error grew by more than `grow`)
+  // 2. history bookkeeping (restart when the error grew by more than `grow`)
   if (tid == 0) {
     int cnt = m.hcount[inst], head = m.hhead[inst];
     double best = m.best[inst];
@@ -136,18 +127,19 @@ __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
   const int cnt = sh_ctl[0], push = sh_ctl[2], h = sh_ctl[3];
   if (push) {
     for (int j = tid; j < N; j += MIX_THREADS) {
-      hdg[(long long)h * N + j] = gcur[j] - gprev[j];
+      hdg[(long long)h * N + j] = graw[j] - gprev[j];
       hdx[(long long)h * N + j] = w[j + 1] - wprev[j];
     }
   }
   __syncthreads();
-  // 4. new Gram row <dg_h, dg_s> and right-hand side <dg_s, g>
+  // 3. least squares on the raw mixing residual r: new Gram row <dr_h, dr_s>
+  //    and right-hand side <dr_s, r>
   if (cnt > 0) {
     double pb[MAXD], pg[MAXD];
 #pragma unroll
     for (int t = 0; t < MAXD; t++) { pb[t] = 0.0; pg[t] = 0.0; }
     for (int j = tid; j < N; j += MIX_THREADS) {
-      const double gv = gcur[j];
+      const double gv = graw[j];
       const double dh = push ? hdg[(long long)h * N + j] : 0.0;
 #pragma unroll
       for (int t = 0; t < MAXD; t++) {
@@ -186,24 +178,35 @@ __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
     }
     __syncthreads();
   }
-  // 5. update w <- w + beta g - sum_s gam_s (dx_s + beta dg_s), clipped in max norm
+  // 4. mixed residual rbar = r - sum_s gam_s dr_s (into gcur)
+  for (int j = tid; j < N; j += MIX_THREADS) {
+    double rb = graw[j];
+    for (int t = 0; t < cnt; t++) rb -= gam[t] * hdg[(long long)sh_slot[t] * N + j];
+    gcur[j] = rb;
+  }
+  __syncthreads();
+  // 5. update w <- w - sum_s gam_s dx_s + beta (1 + a (-d2/dx2)) rbar, clipped in max norm
+  //    (the preconditioner acts on the step only, so FP32 rounding noise it
+  //    amplifies never enters the least squares)
   double dm = 0.0;
   for (int j = tid; j < N; j += MIX_THREADS) {
-    double d = m.beta * gcur[j];
-    for (int t = 0; t < cnt; t++) {
-      const long long o = (long long)sh_slot[t] * N + j;
-      d -= gam[t] * (hdx[o] + m.beta * hdg[o]);
-    }
-    graw[j] = d;
+    const double gc = gcur[j];
+    const double gm = (j > 0) ? gcur[j - 1] : 0.0, gp = (j < N - 1) ? gcur[j + 1] : 0.0;
+    const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
+    const double lap = ((gc - gm) / a1 + (gc - gp) / a2) / (0.5 * (a1 + a2));
+    double d = m.beta * (gc + m.precond * lap);
+    for (int t = 0; t < cnt; t++) d -= gam[t] * hdx[(long long)sh_slot[t] * N + j];
+    wprev[j] = d;  // staged; wprev receives the old field below
     dm = fmax(dm, fabs(d));
   }
   dm = block_max(dm, sm);
   const double scale = (dm > m.clip) ? m.clip / dm : 1.0;
   for (int j = tid; j < N; j += MIX_THREADS) {
     const double wo = w[j + 1];
+    const double d = wprev[j];
     wprev[j] = wo;
-    gprev[j] = gcur[j];
-    w[j + 1] = wo + scale * graw[j];
+    gprev[j] = graw[j];
+    w[j + 1] = wo + scale * d;
   }
   if (tid == 0) {
     m.iters[inst] = it + 1;

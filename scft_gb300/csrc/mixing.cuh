@@ -19,7 +19,7 @@ struct MixDev {
   int *iters;
   double *err;     // ||phi - f0||_inf of the last evaluation
   double *best;    // best error since the last restart
-  double *graw, *gcur, *gprev, *wprev;  // interior vectors
+  double *graw, *gcur, *gprev, *wprev;  // interior vectors: residual, mixed residual, previous residual / field
   double *hdx, *hdg;                    // history of field / residual differences
   double *gram;                         // depth*depth per instance
   int *hcount, *hhead;

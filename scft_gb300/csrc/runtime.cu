@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "mixing.cuh"
+#include "batch.cuh"
 #include "propagate_launch.cuh"
 #include "scft.h"
 
@@ -79,6 +80,7 @@ using namespace scft;
 // ---------------------------------------------------------------------------
 static thread_local std::string g_err = "";
 static std::atomic<long long> g_launches{0};
+void scft_count_launches(long long n) { g_launches += n; }
 
 static int set_err(int code, const char *fmt, ...) {
   char buf[512];
@@ -182,47 +184,7 @@ static int quad_table(int nsteps, double ds, int rule, double *qw) {
 // ---------------------------------------------------------------------------
 // batch
 // ---------------------------------------------------------------------------
-struct ClassPlan {
-  int prec = 0, C = 1, NW = 1;
-  std::vector<int> items;
-  int *d_items = nullptr;
-  void *scratch = nullptr;
-  long long slot_elems = 0;
-  int workers = 0, grid = 0, gpc = 1, head = 0;
-};
-
-struct scft_batch {
-  int count = 0;
-  std::vector<int> n, nsteps, rule;
-  std::vector<double> ds;
-  std::vector<long long> node_off, int_off;
-  long long total_nodes = 0, total_int = 0;
-  // device instance data
-  int *d_n = nullptr, *d_nsteps = nullptr, *d_active = nullptr, *d_status = nullptr;
-  double *d_ds = nullptr, *d_x = nullptr, *d_f0 = nullptr, *d_w = nullptr, *d_phi = nullptr;
-  double *d_Q = nullptr, *d_qw = nullptr, *d_w0 = nullptr;
-  long long *d_node_off = nullptr, *d_int_off = nullptr;
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
-  float last_ms = 0.f;
-  int *d_heads = nullptr;
-  int nheads = 0;
-  std::vector<ClassPlan> plans[2];
-  bool planned[2] = {false, false};
-  double plan_frac[2] = {0, 0};
-  std::vector<int> shapeC[2], shapeNW[2];
-  // Anderson state
-  int depth = 0;
-  double *d_graw = nullptr, *d_gcur = nullptr, *d_gprev = nullptr, *d_wprev = nullptr;
-  double *d_hdx = nullptr, *d_hdg = nullptr, *d_gram = nullptr, *d_err = nullptr, *d_best = nullptr;
-  int *d_iters = nullptr, *d_hcount = nullptr, *d_hhead = nullptr, *d_nactive = nullptr;
-  int *h_nactive = nullptr;
-  cudaStream_t st = nullptr;
-  std::vector<cudaStream_t> side;
-  cudaEvent_t ev_fork = nullptr;
-  std::vector<cudaEvent_t> ev_join;
-};
-
-static BatchDev batch_dev(const scft_batch *B) {
+BatchDev batch_dev(const scft_batch *B) {
   BatchDev b;
   b.count = B->count;
   b.n = B->d_n;

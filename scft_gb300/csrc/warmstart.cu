@@ -1,0 +1,594 @@
+// warmstart.cu -- learned warm start: a 1D-conv network mapping (film width L,
+// contour step count, a 256-point resampled mesh coordinate and the target
+// profile on it) to an initial field w0(x), with hand-written forward,
+// backward and Adam kernels.  It has no counterpart in the reference, which
+// reads its initial guesses from files (1D_FEM.c:321-342, scft_util.cc:14-41).
+//
+// Network: NL dilated convolutions over P = 256 grid points, kernel K = 5,
+// dilation 1, 2, 4, 8; channels 4 -> 64 -> 64 -> 64 -> 1; tanh on hidden
+// layers; zero padding.  Weights FP32, hidden activations stored BF16 (or FP32
+// for the gradient check), all accumulations FP32.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "batch.cuh"
+#include "common.cuh"
+#include "scft.h"
+
+namespace scft {
+
+constexpr int WS_P = 256;        // grid points
+constexpr int WS_IN = 4;         // input features
+constexpr int WS_K = 5;          // kernel size
+constexpr int WS_LAYERS = 4;
+constexpr float WS_SCALE = 5.0f; // output scale: w = WS_SCALE * net
+
+struct LayerSpec { int ci, co, dil, act; };
+
+__device__ __forceinline__ float ld_act(const float *p, long long i) { return p[i]; }
+__device__ __forceinline__ float ld_act(const __nv_bfloat16 *p, long long i) { return __bfloat162float(p[i]); }
+__device__ __forceinline__ void st_act(float *p, long long i, float v) { p[i] = v; }
+__device__ __forceinline__ void st_act(__nv_bfloat16 *p, long long i, float v) { p[i] = __float2bfloat16_rn(v); }
+
+// y[b][co][p] = bias[co] + sum_ci sum_k W[co][ci][k] x[b][ci][p + (k-2) d]; tanh if act;
+// if dtanh != nullptr the result is multiplied by (1 - dtanh[b][co][p]^2) (backward use).
+template <int CO_TILE, typename TIN, typename TOUT, typename TD>
+__global__ void __launch_bounds__(WS_P) conv_fwd_kernel(const TIN *__restrict__ x, int ci_n,
+                                                        const float *__restrict__ W,
+                                                        const float *__restrict__ bias, int co_n, int dil,
+                                                        int act, const TD *__restrict__ dtanh,
+                                                        TOUT *__restrict__ y) {
+  extern __shared__ float sm[];
+  const int b = blockIdx.x, co0 = blockIdx.y * CO_TILE, p = threadIdx.x;
+  const int halo = 2 * dil, width = WS_P + 2 * halo;
+  float *xs = sm;                       // ci_n x width
+  float *ws = sm + ci_n * width;        // CO_TILE x ci_n x K
+  for (int i = threadIdx.x; i < ci_n * width; i += WS_P) {
+    const int c = i / width, q = i % width - halo;
+    xs[i] = (q >= 0 && q < WS_P) ? ld_act(x, ((long long)b * ci_n + c) * WS_P + q) : 0.f;
+  }
+  for (int i = threadIdx.x; i < CO_TILE * ci_n * WS_K; i += WS_P) {
+    const int t = i / (ci_n * WS_K), r = i % (ci_n * WS_K);
+    ws[i] = (co0 + t < co_n) ? W[(long long)(co0 + t) * ci_n * WS_K + r] : 0.f;
+  }
+  __syncthreads();
+  float acc[CO_TILE];
+#pragma unroll
+  for (int t = 0; t < CO_TILE; t++) acc[t] = 0.f;
+  for (int c = 0; c < ci_n; c++) {
+    const float *xr = xs + c * width + halo + p;
+    float xv[WS_K];
+#pragma unroll
+    for (int k = 0; k < WS_K; k++) xv[k] = xr[(k - 2) * dil];
+#pragma unroll
+    for (int t = 0; t < CO_TILE; t++) {
+      const float *wr = ws + (t * ci_n + c) * WS_K;
+#pragma unroll
+      for (int k = 0; k < WS_K; k++) acc[t] = fmaf(wr[k], xv[k], acc[t]);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < CO_TILE; t++) {
+    const int co = co0 + t;
+    if (co >= co_n) break;
+    float v = acc[t] + (bias ? bias[co] : 0.f);
+    if (act) v = tanhf(v);
+    const long long o = ((long long)b * co_n + co) * WS_P + p;
+    if (dtanh) {
+      const float a = ld_act(dtanh, o);
+      v *= (1.f - a * a);
+    }
+    st_act(y, o, v);
+  }
+}
+
+// gW[co][ci][k] = sum_b sum_p gy[b][co][p] x[b][ci][p + (k-2) d];  gb[co] = sum gy (ci == 0 blocks)
+template <typename TIN>
+__global__ void __launch_bounds__(256) conv_wgrad_kernel(const float *__restrict__ gy, const TIN *__restrict__ x,
+                                                         int B, int ci_n, int co_n, int dil,
+                                                         float *__restrict__ gW, float *__restrict__ gb) {
+  const int co = blockIdx.x, ci = blockIdx.y;
+  float acc[WS_K + 1];
+#pragma unroll
+  for (int k = 0; k <= WS_K; k++) acc[k] = 0.f;
+  const long long total = (long long)B * WS_P;
+  for (long long idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int b = (int)(idx / WS_P), p = (int)(idx % WS_P);
+    const float g = gy[((long long)b * co_n + co) * WS_P + p];
+    const long long xb = ((long long)b * ci_n + ci) * WS_P;
+#pragma unroll
+    for (int k = 0; k < WS_K; k++) {
+      const int q = p + (k - 2) * dil;
+      if (q >= 0 && q < WS_P) acc[k] = fmaf(g, ld_act(x, xb + q), acc[k]);
+    }
+    acc[WS_K] += g;
+  }
+  __shared__ float red[WS_K + 1][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k <= WS_K; k++) {
+    float v = acc[k];
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+    if (lane == 0) red[k][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x <= WS_K) {
+    float v = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[threadIdx.x][w];
+    if (threadIdx.x < WS_K) gW[((long long)co * ci_n + ci) * WS_K + threadIdx.x] = v;
+    else if (ci == 0) gb[co] = v;
+  }
+}
+
+// W'[ci][co][k] = W[co][ci][K-1-k]  (weights of the data-gradient convolution)
+__global__ void flip_transpose_kernel(const float *W, int ci_n, int co_n, float *Wt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ci_n * co_n * WS_K) return;
+  const int k = i % WS_K, co = (i / WS_K) % co_n, ci = i / (WS_K * co_n);
+  Wt[i] = W[((long long)co * ci_n + ci) * WS_K + (WS_K - 1 - k)];
+}
+
+// MSE loss of out against target (both B x P), gradient into g, partial sums into loss[0]
+__global__ void mse_kernel(const float *out, const float *tgt, long long n, float *g, double *loss) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float d = out[i] - tgt[i];
+    g[i] = 2.f * d / (float)n;
+    s += (double)d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    atomicAdd(loss, t / (double)n);
+  }
+}
+
+__global__ void adam_kernel(float *p, const float *g, float *m, float *v, int n, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void gather_rows_kernel(const float *src, const int *idx, int rows, int row_len, float *dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)rows * row_len) return;
+  const int r = (int)(i / row_len), c = (int)(i % row_len);
+  dst[i] = src[(long long)idx[r] * row_len + c];
+}
+
+// linear interpolation of nodal values f (mesh x, n nodes) at position xq
+__device__ double interp_mesh(const double *x, const double *f, int n, double xq) {
+  if (xq <= x[0]) return f[0];
+  if (xq >= x[n - 1]) return f[n - 1];
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (x[mid] <= xq) lo = mid;
+    else hi = mid;
+  }
+  const double t = (xq - x[lo]) / (x[hi] - x[lo]);
+  return f[lo] + t * (f[hi] - f[lo]);
+}
+
+struct WsBatchView {
+  const int *n, *nsteps;
+  const long long *node_off;
+  const double *x, *f0;
+  double *w;
+};
+
+// Network input of instance i on the 256-point grid u_k = k/255:
+//   [2u-1, (L-6)/4, (log2 nsteps - 10.5)/1.5, ln(max(f0(x_k), 1e-8))/10]
+// and (tgt != nullptr) the target w(x_k)/5 interpolated from the instance's field.
+__global__ void features_kernel(WsBatchView v, const int *sel, int B, float *feat, float *tgt) {
+  const int b = blockIdx.x, k = threadIdx.x;
+  if (b >= B) return;
+  const int i = sel ? sel[b] : b;
+  const int n = v.n[i];
+  const long long off = v.node_off[i];
+  const double *x = v.x + off;
+  const double L = x[n - 1] - x[0];
+  const double u = (double)k / (WS_P - 1);
+  const double xq = x[0] + u * L;
+  const double f0 = interp_mesh(x, v.f0 + off, n, xq);
+  float *fb = feat + (long long)b * WS_IN * WS_P;
+  fb[0 * WS_P + k] = (float)(2.0 * u - 1.0);
+  fb[1 * WS_P + k] = (float)((L - 6.0) / 4.0);
+  fb[2 * WS_P + k] = (float)((log2((double)v.nsteps[i]) - 10.5) / 1.5);
+  fb[3 * WS_P + k] = (float)(log(fmax(f0, 1e-8)) / 10.0);
+  if (tgt) tgt[(long long)b * WS_P + k] = (float)(interp_mesh(x, v.w + off, n, xq) / WS_SCALE);
+}
+
+// fields of every instance from the network output on the grid (linear interpolation)
+__global__ void predict_fields_kernel(WsBatchView v, const float *out, int B) {
+  const int b = blockIdx.x;
+  if (b >= B) return;
+  const int n = v.n[b];
+  const long long off = v.node_off[b];
+  const double *x = v.x + off;
+  const double L = x[n - 1] - x[0];
+  const float *o = out + (long long)b * WS_P;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double val = 0.0;
+    if (j > 0 && j < n - 1) {
+      const double s = (x[j] - x[0]) / L * (WS_P - 1);
+      int k0 = (int)floor(s);
+      k0 = k0 < 0 ? 0 : (k0 > WS_P - 2 ? WS_P - 2 : k0);
+      const double t = s - k0;
+      val = WS_SCALE * ((1.0 - t) * o[k0] + t * o[k0 + 1]);
+    }
+    v.w[off + j] = val;
+  }
+}
+
+}  // namespace scft
+
+using namespace scft;
+
+namespace {
+const LayerSpec kLayers[WS_LAYERS] = {{WS_IN, 64, 1, 1}, {64, 64, 2, 1}, {64, 64, 4, 1}, {64, 1, 8, 0}};
+
+size_t conv_smem(int ci, int dil, int co_tile) {
+  return sizeof(float) * ((size_t)ci * (WS_P + 4 * dil) + (size_t)co_tile * ci * WS_K);
+}
+}  // namespace
+
+struct scft_ws {
+  int bf16 = 1;
+  int nparam = 0;
+  int poff[WS_LAYERS], boff[WS_LAYERS];
+  float *d_p = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr, *d_wt = nullptr;
+  int adam_t = 0;
+  int cap = 0;
+  float *d_feat = nullptr, *d_tgt = nullptr, *d_out = nullptr, *d_gout = nullptr;
+  void *d_act[WS_LAYERS - 1] = {nullptr, nullptr, nullptr};
+  float *d_ga = nullptr, *d_gb = nullptr;
+  double *d_loss = nullptr;
+  int *d_idx = nullptr;
+  float *d_dsf = nullptr, *d_dst = nullptr;
+  int nds = 0;
+  cudaStream_t st = nullptr;
+};
+
+void scft_count_launches(long long n);
+
+static int ws_err(int code, const char *msg);
+
+#define WCK(call)                                                        \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) return ws_err(SCFT_ECUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+static int ws_reserve(scft_ws *W, int B) {
+  if (B <= W->cap) return SCFT_OK;
+  cudaFree(W->d_feat); cudaFree(W->d_tgt); cudaFree(W->d_out); cudaFree(W->d_gout);
+  for (auto &a : W->d_act) cudaFree(a);
+  cudaFree(W->d_ga); cudaFree(W->d_gb); cudaFree(W->d_idx);
+  const size_t P = WS_P, esz = W->bf16 ? 2 : 4;
+  WCK(cudaMalloc(&W->d_feat, sizeof(float) * B * WS_IN * P));
+  WCK(cudaMalloc(&W->d_tgt, sizeof(float) * B * P));
+  WCK(cudaMalloc(&W->d_out, sizeof(float) * B * P));
+  WCK(cudaMalloc(&W->d_gout, sizeof(float) * B * P));
+  for (auto &a : W->d_act) WCK(cudaMalloc(&a, esz * B * 64 * P));
+  WCK(cudaMalloc(&W->d_ga, sizeof(float) * B * 64 * P));
+  WCK(cudaMalloc(&W->d_gb, sizeof(float) * B * 64 * P));
+  WCK(cudaMalloc(&W->d_idx, sizeof(int) * B));
+  W->cap = B;
+  return SCFT_OK;
+}
+
+template <int CT, typename TIN, typename TOUT, typename TD>
+static cudaError_t conv(const TIN *x, int ci, const float *w, const float *bias, int co, int dil, int act,
+                        const TD *dtanh, TOUT *y, int B, cudaStream_t st) {
+  const size_t sm = conv_smem(ci, dil, CT);
+  auto kern = conv_fwd_kernel<CT, TIN, TOUT, TD>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  dim3 grid(B, (co + CT - 1) / CT);
+  kern<<<grid, WS_P, sm, st>>>(x, ci, w, bias, co, dil, act, dtanh, y);
+  scft_count_launches(1);
+  return cudaGetLastError();
+}
+
+// forward pass of B samples whose features are in d_feat; output in d_out
+template <typename TA>
+static int ws_forward_dev(scft_ws *W, int B) {
+  TA *a1 = (TA *)W->d_act[0], *a2 = (TA *)W->d_act[1], *a3 = (TA *)W->d_act[2];
+  const float *p = W->d_p;
+  const float *nul = nullptr;
+  WCK((conv<16, float, TA, float>(W->d_feat, 4, p + W->poff[0], p + W->boff[0], 64, 1, 1, nul, a1, B, W->st)));
+  WCK((conv<16, TA, TA, float>(a1, 64, p + W->poff[1], p + W->boff[1], 64, 2, 1, nul, a2, B, W->st)));
+  WCK((conv<16, TA, TA, float>(a2, 64, p + W->poff[2], p + W->boff[2], 64, 4, 1, nul, a3, B, W->st)));
+  WCK((conv<1, TA, float, float>(a3, 64, p + W->poff[3], p + W->boff[3], 1, 8, 0, nul, W->d_out, B, W->st)));
+  return SCFT_OK;
+}
+
+// loss and gradient of B samples (features d_feat, targets d_tgt) into d_g and d_loss[slot]
+template <typename TA>
+static int ws_backward_dev(scft_ws *W, int B, int slot) {
+  TA *a1 = (TA *)W->d_act[0], *a2 = (TA *)W->d_act[1], *a3 = (TA *)W->d_act[2];
+  const float *p = W->d_p;
+  float *g = W->d_g;
+  const long long n = (long long)B * WS_P;
+  mse_kernel<<<std::min<long long>(1024, (n + 255) / 256), 256, 0, W->st>>>(W->d_out, W->d_tgt, n, W->d_gout,
+                                                                         W->d_loss + slot);
+  scft_count_launches(1);
+  // layer 3 (64 -> 1, linear)
+  conv_wgrad_kernel<TA><<<dim3(1, 64), 256, 0, W->st>>>(W->d_gout, a3, B, 64, 1, 8, g + W->poff[3], g + W->boff[3]);
+  flip_transpose_kernel<<<(64 * 1 * WS_K + 255) / 256, 256, 0, W->st>>>(p + W->poff[3], 64, 1, W->d_wt);
+  scft_count_launches(2);
+  WCK((conv<16, float, float, TA>(W->d_gout, 1, W->d_wt, nullptr, 64, 8, 0, a3, W->d_ga, B, W->st)));
+  // layer 2 (64 -> 64, dilation 4)
+  conv_wgrad_kernel<TA><<<dim3(64, 64), 256, 0, W->st>>>(W->d_ga, a2, B, 64, 64, 4, g + W->poff[2], g + W->boff[2]);
+  flip_transpose_kernel<<<(64 * 64 * WS_K + 255) / 256, 256, 0, W->st>>>(p + W->poff[2], 64, 64, W->d_wt);
+  scft_count_launches(2);
+  WCK((conv<16, float, float, TA>(W->d_ga, 64, W->d_wt, nullptr, 64, 4, 0, a2, W->d_gb, B, W->st)));
+  // layer 1 (64 -> 64, dilation 2)
+  conv_wgrad_kernel<TA><<<dim3(64, 64), 256, 0, W->st>>>(W->d_gb, a1, B, 64, 64, 2, g + W->poff[1], g + W->boff[1]);
+  flip_transpose_kernel<<<(64 * 64 * WS_K + 255) / 256, 256, 0, W->st>>>(p + W->poff[1], 64, 64, W->d_wt);
+  scft_count_launches(2);
+  WCK((conv<16, float, float, TA>(W->d_gb, 64, W->d_wt, nullptr, 64, 2, 0, a1, W->d_ga, B, W->st)));
+  // layer 0 (4 -> 64)
+  conv_wgrad_kernel<float><<<dim3(64, 4), 256, 0, W->st>>>(W->d_ga, W->d_feat, B, 4, 64, 1, g + W->poff[0], g + W->boff[0]);
+  scft_count_launches(1);
+  WCK(cudaGetLastError());
+  return SCFT_OK;
+}
+
+static int ws_forward(scft_ws *W, int B) {
+  return W->bf16 ? ws_forward_dev<__nv_bfloat16>(W, B) : ws_forward_dev<float>(W, B);
+}
+static int ws_backward(scft_ws *W, int B, int slot) {
+  return W->bf16 ? ws_backward_dev<__nv_bfloat16>(W, B, slot) : ws_backward_dev<float>(W, B, slot);
+}
+
+static WsBatchView ws_view(scft_batch *b) {
+  WsBatchView v;
+  v.n = b->d_n;
+  v.nsteps = b->d_nsteps;
+  v.node_off = b->d_node_off;
+  v.x = b->d_x;
+  v.f0 = b->d_f0;
+  v.w = b->d_w;
+  return v;
+}
+
+static thread_local std::string g_ws_err;
+static int ws_err(int code, const char *msg) {
+  g_ws_err = msg;
+  return code;
+}
+
+extern "C" {
+
+int scft_ws_create(int act_bf16, unsigned long long seed, scft_ws **out) {
+  if (!out) return ws_err(SCFT_EINVAL, "scft_ws_create: null output");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return ws_err(SCFT_ENODEV, "no CUDA device");
+  }
+  scft_ws *W = new scft_ws();
+  W->bf16 = act_bf16 ? 1 : 0;
+  int off = 0;
+  for (int l = 0; l < WS_LAYERS; l++) {
+    W->poff[l] = off;
+    off += kLayers[l].co * kLayers[l].ci * WS_K;
+    W->boff[l] = off;
+    off += kLayers[l].co;
+  }
+  W->nparam = off;
+  std::vector<float> h(off, 0.f);
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l < WS_LAYERS; l++) {
+    const double fan_in = kLayers[l].ci * WS_K, fan_out = kLayers[l].co * WS_K;
+    double lim = std::sqrt(6.0 / (fan_in + fan_out));
+    if (l == WS_LAYERS - 1) lim *= 0.1;
+    std::uniform_real_distribution<double> U(-lim, lim);
+    for (int i = 0; i < kLayers[l].co * kLayers[l].ci * WS_K; i++) h[W->poff[l] + i] = (float)U(rng);
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&W->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&W->d_p, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&W->d_g, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&W->d_m, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&W->d_v, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&W->d_wt, sizeof(float) * 64 * 64 * WS_K);
+  if (e == cudaSuccess) e = cudaMalloc(&W->d_loss, sizeof(double) * 65536);
+  if (e == cudaSuccess) e = cudaMemcpy(W->d_p, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(W->d_m, 0, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMemset(W->d_v, 0, sizeof(float) * off);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return ws_err(SCFT_ECUDA, cudaGetErrorString(e));
+  }
+  *out = W;
+  return SCFT_OK;
+}
+
+int scft_ws_destroy(scft_ws *W) {
+  if (!W) return SCFT_OK;
+  if (W->st) cudaStreamSynchronize(W->st);
+  cudaFree(W->d_p); cudaFree(W->d_g); cudaFree(W->d_m); cudaFree(W->d_v); cudaFree(W->d_wt);
+  cudaFree(W->d_loss); cudaFree(W->d_feat); cudaFree(W->d_tgt); cudaFree(W->d_out); cudaFree(W->d_gout);
+  for (auto &a : W->d_act) cudaFree(a);
+  cudaFree(W->d_ga); cudaFree(W->d_gb); cudaFree(W->d_idx); cudaFree(W->d_dsf); cudaFree(W->d_dst);
+  if (W->st) cudaStreamDestroy(W->st);
+  delete W;
+  return SCFT_OK;
+}
+
+int scft_ws_param_count(scft_ws *W) { return W ? W->nparam : SCFT_EINVAL; }
+
+int scft_ws_get_params(scft_ws *W, float *out) {
+  if (!W || !out) return ws_err(SCFT_EINVAL, "scft_ws_get_params");
+  WCK(cudaMemcpy(out, W->d_p, sizeof(float) * W->nparam, cudaMemcpyDeviceToHost));
+  return SCFT_OK;
+}
+
+int scft_ws_set_params(scft_ws *W, const float *in) {
+  if (!W || !in) return ws_err(SCFT_EINVAL, "scft_ws_set_params");
+  WCK(cudaMemcpy(W->d_p, in, sizeof(float) * W->nparam, cudaMemcpyHostToDevice));
+  W->adam_t = 0;
+  WCK(cudaMemset(W->d_m, 0, sizeof(float) * W->nparam));
+  WCK(cudaMemset(W->d_v, 0, sizeof(float) * W->nparam));
+  return SCFT_OK;
+}
+
+int scft_ws_forward(scft_ws *W, const float *features, int B, float *out) {
+  if (!W || !features || !out || B <= 0) return ws_err(SCFT_EINVAL, "scft_ws_forward");
+  int rc = ws_reserve(W, B);
+  if (rc) return rc;
+  WCK(cudaMemcpyAsync(W->d_feat, features, sizeof(float) * B * WS_IN * WS_P, cudaMemcpyHostToDevice, W->st));
+  if ((rc = ws_forward(W, B))) return rc;
+  WCK(cudaMemcpyAsync(out, W->d_out, sizeof(float) * B * WS_P, cudaMemcpyDeviceToHost, W->st));
+  WCK(cudaStreamSynchronize(W->st));
+  return SCFT_OK;
+}
+
+int scft_ws_loss_grad(scft_ws *W, const float *features, const float *targets, int B, double *loss, float *grad) {
+  if (!W || !features || !targets || B <= 0) return ws_err(SCFT_EINVAL, "scft_ws_loss_grad");
+  int rc = ws_reserve(W, B);
+  if (rc) return rc;
+  WCK(cudaMemcpyAsync(W->d_feat, features, sizeof(float) * B * WS_IN * WS_P, cudaMemcpyHostToDevice, W->st));
+  WCK(cudaMemcpyAsync(W->d_tgt, targets, sizeof(float) * B * WS_P, cudaMemcpyHostToDevice, W->st));
+  WCK(cudaMemsetAsync(W->d_loss, 0, sizeof(double), W->st));
+  if ((rc = ws_forward(W, B)) || (rc = ws_backward(W, B, 0))) return rc;
+  if (grad) WCK(cudaMemcpyAsync(grad, W->d_g, sizeof(float) * W->nparam, cudaMemcpyDeviceToHost, W->st));
+  if (loss) WCK(cudaMemcpyAsync(loss, W->d_loss, sizeof(double), cudaMemcpyDeviceToHost, W->st));
+  WCK(cudaStreamSynchronize(W->st));
+  return SCFT_OK;
+}
+
+int scft_ws_batch_features(scft_batch *b, float *features, float *targets) {
+  if (!b || !features) return ws_err(SCFT_EINVAL, "scft_ws_batch_features");
+  float *df = nullptr, *dt = nullptr;
+  WCK(cudaMalloc(&df, sizeof(float) * b->count * WS_IN * WS_P));
+  if (targets) WCK(cudaMalloc(&dt, sizeof(float) * b->count * WS_P));
+  features_kernel<<<b->count, WS_P, 0, b->st>>>(ws_view(b), nullptr, b->count, df, dt);
+  scft_count_launches(1);
+  WCK(cudaGetLastError());
+  WCK(cudaMemcpyAsync(features, df, sizeof(float) * b->count * WS_IN * WS_P, cudaMemcpyDeviceToHost, b->st));
+  if (targets) WCK(cudaMemcpyAsync(targets, dt, sizeof(float) * b->count * WS_P, cudaMemcpyDeviceToHost, b->st));
+  WCK(cudaStreamSynchronize(b->st));
+  cudaFree(df);
+  cudaFree(dt);
+  return SCFT_OK;
+}
+
+int scft_ws_dataset_from_batch(scft_ws *W, scft_batch *b, const int *mask) {
+  if (!W || !b) return ws_err(SCFT_EINVAL, "scft_ws_dataset_from_batch");
+  std::vector<int> sel;
+  for (int i = 0; i < b->count; i++)
+    if (!mask || mask[i]) sel.push_back(i);
+  if (sel.empty()) return ws_err(SCFT_EINVAL, "scft_ws_dataset_from_batch: empty selection");
+  const int n = (int)sel.size(), old = W->nds;
+  float *nf = nullptr, *nt = nullptr;
+  int *ds = nullptr;
+  WCK(cudaMalloc(&nf, sizeof(float) * (size_t)(old + n) * WS_IN * WS_P));
+  WCK(cudaMalloc(&nt, sizeof(float) * (size_t)(old + n) * WS_P));
+  WCK(cudaMalloc(&ds, sizeof(int) * n));
+  if (old) {
+    WCK(cudaMemcpyAsync(nf, W->d_dsf, sizeof(float) * (size_t)old * WS_IN * WS_P, cudaMemcpyDeviceToDevice, b->st));
+    WCK(cudaMemcpyAsync(nt, W->d_dst, sizeof(float) * (size_t)old * WS_P, cudaMemcpyDeviceToDevice, b->st));
+  }
+  WCK(cudaMemcpyAsync(ds, sel.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
+  features_kernel<<<n, WS_P, 0, b->st>>>(ws_view(b), ds, n, nf + (size_t)old * WS_IN * WS_P, nt + (size_t)old * WS_P);
+  scft_count_launches(1);
+  WCK(cudaGetLastError());
+  WCK(cudaStreamSynchronize(b->st));
+  cudaFree(ds);
+  cudaFree(W->d_dsf);
+  cudaFree(W->d_dst);
+  W->d_dsf = nf;
+  W->d_dst = nt;
+  W->nds = old + n;
+  return W->nds;
+}
+
+int scft_ws_train(scft_ws *W, int steps, int batch, float lr, unsigned long long seed, float *losses) {
+  if (!W || steps <= 0 || batch <= 0 || steps > 65536) return ws_err(SCFT_EINVAL, "scft_ws_train");
+  if (W->nds <= 0) return ws_err(SCFT_EINVAL, "scft_ws_train: no dataset");
+  int rc = ws_reserve(W, batch);
+  if (rc) return rc;
+  std::mt19937_64 rng(seed);
+  std::vector<int> perm(W->nds), idx(batch);
+  for (int i = 0; i < W->nds; i++) perm[i] = i;
+  size_t pos = W->nds;
+  int *h_idx = nullptr;
+  WCK(cudaMallocHost(&h_idx, sizeof(int) * batch * 2));
+  WCK(cudaMemsetAsync(W->d_loss, 0, sizeof(double) * steps, W->st));
+  const float b1 = 0.9f, b2 = 0.999f;
+  for (int s = 0; s < steps; s++) {
+    int *hb = h_idx + (s & 1) * batch;
+    for (int k = 0; k < batch; k++) {
+      if (pos >= perm.size()) { std::shuffle(perm.begin(), perm.end(), rng); pos = 0; }
+      hb[k] = perm[pos++];
+    }
+    WCK(cudaStreamSynchronize(W->st));  // the staging buffer of step s-2 is free again
+    WCK(cudaMemcpyAsync(W->d_idx, hb, sizeof(int) * batch, cudaMemcpyHostToDevice, W->st));
+    const long long nf = (long long)batch * WS_IN * WS_P, nt = (long long)batch * WS_P;
+    gather_rows_kernel<<<(unsigned)((nf + 255) / 256), 256, 0, W->st>>>(W->d_dsf, W->d_idx, batch, WS_IN * WS_P, W->d_feat);
+    gather_rows_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, W->st>>>(W->d_dst, W->d_idx, batch, WS_P, W->d_tgt);
+    scft_count_launches(2);
+    if ((rc = ws_forward(W, batch)) || (rc = ws_backward(W, batch, s))) { cudaFreeHost(h_idx); return rc; }
+    W->adam_t++;
+    const float c1 = 1.f - std::pow(b1, (float)W->adam_t), c2 = 1.f - std::pow(b2, (float)W->adam_t);
+    adam_kernel<<<(W->nparam + 255) / 256, 256, 0, W->st>>>(W->d_p, W->d_g, W->d_m, W->d_v, W->nparam, lr, b1, b2,
+                                                            1e-8f, c1, c2);
+    scft_count_launches(1);
+    WCK(cudaGetLastError());
+  }
+  WCK(cudaStreamSynchronize(W->st));
+  cudaFreeHost(h_idx);
+  if (losses) {
+    std::vector<double> l(steps);
+    WCK(cudaMemcpy(l.data(), W->d_loss, sizeof(double) * steps, cudaMemcpyDeviceToHost));
+    for (int s = 0; s < steps; s++) losses[s] = (float)l[s];
+  }
+  return SCFT_OK;
+}
+
+int scft_ws_predict(scft_ws *W, scft_batch *b) {
+  if (!W || !b) return ws_err(SCFT_EINVAL, "scft_ws_predict");
+  int rc = ws_reserve(W, b->count);
+  if (rc) return rc;
+  // the network runs on the batch's stream so that a following solve is ordered after it
+  cudaStream_t keep = W->st;
+  W->st = b->st;
+  WCK(cudaEventRecord(b->t0, b->st));
+  features_kernel<<<b->count, WS_P, 0, b->st>>>(ws_view(b), nullptr, b->count, W->d_feat, nullptr);
+  scft_count_launches(1);
+  rc = ws_forward(W, b->count);
+  if (!rc) {
+    predict_fields_kernel<<<b->count, 128, 0, b->st>>>(ws_view(b), W->d_out, b->count);
+    scft_count_launches(1);
+  }
+  W->st = keep;
+  if (rc) return rc;
+  WCK(cudaGetLastError());
+  WCK(cudaEventRecord(b->t1, b->st));
+  WCK(cudaEventSynchronize(b->t1));
+  WCK(cudaEventElapsedTime(&b->last_ms, b->t0, b->t1));
+  return SCFT_OK;
+}
+
+const char *scft_ws_last_error(void) { return g_ws_err.c_str(); }
+
+}  // extern "C"
