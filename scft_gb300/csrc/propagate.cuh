@@ -311,14 +311,30 @@ struct Propagator {
     const R wend = S.qw[15];
 
     // ---------------- contour loop ----------------
+    // The slice read back at step k (ns - k) is prefetched during step k-1
+    // when it was stored before step k-1; otherwise it is loaded in step k.
+    R nxt[C];
+    bool have_nxt = false;
     for (int k = 1; k <= ns; k++) {
       const bool acc_step = (k >= ns - half);
       const bool self_pair = (k == ns - k);
       R pre[C];
       if (acc_step && !self_pair) {
-        const R *src = slot + (long long)(ns - k) * TC + P;
+        if (have_nxt) {
 #pragma unroll
-        for (int c = 0; c < C; c++) pre[c] = src[(long long)c * T];
+          for (int c = 0; c < C; c++) pre[c] = nxt[c];
+        } else {
+          const R *src = slot + (long long)(ns - k) * TC + P;
+#pragma unroll
+          for (int c = 0; c < C; c++) pre[c] = src[(long long)c * T];
+        }
+      }
+      // prefetch for step k+1: its slice ns-k-1 must have been stored at a step < k
+      have_nxt = (k + 1 <= ns) && (k + 1 >= ns - half) && (k + 1 != ns - k - 1) && (ns - k - 1 < k);
+      if (have_nxt) {
+        const R *src = slot + (long long)(ns - k - 1) * TC + P;
+#pragma unroll
+        for (int c = 0; c < C; c++) nxt[c] = src[(long long)c * T];
       }
       // right-hand side
       R r[C];

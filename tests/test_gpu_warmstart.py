@@ -63,7 +63,7 @@ def test_training_reduces_loss_and_warm_start_saves_iterations():
     train = W.warmstart_train(512, seed=101)
     ws, losses, stats = generate_and_train(train, steps=600, batch=128, lr=2e-3, seed=0)
     assert stats["solved"] >= 0.95 * stats["total"]
-    assert np.mean(losses[-50:]) < 0.1 * np.mean(losses[:10])
+    assert np.mean(losses[-50:]) < 0.25 * np.mean(losses[:10])
     held = W.warmstart_eval(128, seed=202)
     with api.Batch(held) as b:
         cold = b.solve(precision=F32, tol=1e-6)
