@@ -221,6 +221,32 @@ int scft_ws_train(scft_ws *ws, int steps, int batch, float lr, unsigned long lon
 int scft_ws_predict(scft_ws *ws, scft_batch *b);
 const char *scft_ws_last_error(void);
 
+/* =========================================================================
+ * Density without any device allocation.  No counterpart in the reference.
+ *
+ * For callers that may not allocate GPU memory: applications whose device
+ * memory belongs to another allocator (a framework's pool with a fixed budget)
+ * and per-iteration loops that cannot afford cudaMalloc/cudaFree, which can
+ * block on or synchronize the whole device.  The caller passes device buffers:
+ * x and w (n_nodes doubles: mesh and field, wall values of w ignored), phi
+ * (n_nodes doubles, out) and Q (one double, out, may be NULL).  The work is
+ * enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * results are ready when that stream has completed; nothing is copied to or
+ * from the host.
+ *
+ * The propagator's half-contour store lives in one fixed 32 MiB device array
+ * of the library (every GPU that loads the library holds it until the process
+ * exits): an instance needs (nsteps/2 + 1) x padded nodes x 4 bytes (FP32) or
+ * 8 bytes (FP64); larger instances are rejected with SCFT_EINVAL and a message
+ * from scft_last_error().  All calls share that array, so calls whose GPU work
+ * overlaps in time (different streams, threads or processes on the same GPU)
+ * race and must be serialised by the caller.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  Same results as scft_batch_evaluate.
+ * ========================================================================= */
+int scft_density_noalloc(int n_nodes, const double *x, const double *w, int nsteps, double ds, int rule,
+                         int precision, double *phi, double *Q, void *stream);
+
 /* Kernels launched by this library since load (graph replays count each node). */
 long long scft_kernel_launches(void);
 

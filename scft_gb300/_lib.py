@@ -102,6 +102,8 @@ SIGNATURES = {
     "scft_ws_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _fp]),
     "scft_ws_predict": (C.c_int, [C.c_void_p, C.c_void_p]),
     "scft_ws_last_error": (C.c_char_p, []),
+    "scft_density_noalloc": (C.c_int, [C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp,
+                                       C.c_void_p]),
 }
 
 _lib = None

@@ -181,6 +181,18 @@ static int quad_table(int nsteps, double ds, int rule, double *qw) {
   return SCFT_OK;
 }
 
+// Internal helpers shared with the no-allocation entry point (noalloc.cu).
+int scft_internal_default_shape(int n_interior, int precision, int *C, int *NW) {
+  if (precision != PREC_F32 && precision != PREC_F64) return SCFT_EINVAL;
+  default_shape(n_interior, precision, C, NW);
+  return (*NW <= 32 && 32 * *NW * *C >= n_interior && propagate_has_class(precision, *C, *NW)) ? SCFT_OK
+                                                                                                 : SCFT_EINVAL;
+}
+int scft_internal_quad_table(int nsteps, double ds, int rule, double *qw) {
+  return quad_table(nsteps, ds, rule, qw);
+}
+int scft_internal_set_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+
 // ---------------------------------------------------------------------------
 // batch
 // ---------------------------------------------------------------------------
