@@ -29,6 +29,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -287,6 +289,8 @@ def ours_arm(args):
         step_ms.append(t_start + b.last_ms())
         conv.append(int(((r["status"] & ST_CONVERGED) != 0).sum()))
         iters.append(float(r["iterations"].mean()))
+    its_last = r["iterations"]
+    tr_active, tr_ms = b.trace()
     torch.cuda.synchronize()
     launches = api.kernel_launches() - l0
     clk = clocks.stop()
@@ -331,6 +335,10 @@ def ours_arm(args):
                    "parallelism": f"replicas x{world}, batch split by cost"},
         "gpu_launches": launches,
         "iterations_mean": statistics.mean(iters),
+        "iterations_pct": {q: float(np.percentile(its_last, q)) for q in (50, 90, 99, 100)},
+        "tail": {"ms_until_90pct_done": float(tr_ms[int(np.argmax(tr_active <= 0.1 * len(mine)))])
+                 if len(tr_ms) and (tr_active <= 0.1 * len(mine)).any() else None,
+                 "ms_total_host": float(tr_ms[-1]) if len(tr_ms) else None},
         "converged_per_step": conv_all,
         "clocks": clk,
         "roofline": roofline,
@@ -383,6 +391,23 @@ def ours_arm(args):
     return 0
 
 
+def profile_pass(args):
+    """One FP32 propagator pass over the workload after one warm-up pass: the
+    small, self-contained command the ncu captures run."""
+    import torch
+
+    from scft_gb300 import F32, api
+
+    insts, _ = make_workload(args.workload, args.count)
+    with api.Batch(insts) as b:
+        for _ in range(2):
+            b.evaluate(F32)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_pass": args.workload, "instances": len(insts), "ms": b.last_ms(),
+                          "classes": b.profile(F32)}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -398,7 +423,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-pass", action="store_true", help="one FP32 propagator pass (for ncu)")
     args = ap.parse_args()
+    if args.profile_pass:
+        return profile_pass(args)
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     return reference_arm(args) if args.impl == "reference" else ours_arm(args)

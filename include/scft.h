@@ -118,7 +118,8 @@ typedef struct scft_instance {
   const double *x;    /* n_nodes coordinates or NULL (uniform on [0, L]) */
   double L;
   const double *f0;   /* n_nodes target density */
-  const double *w0;   /* n_nodes initial field or NULL (zero); wall values ignored */
+  const double *w0;   /* n_nodes initial field or NULL (zero); wall values are kept but never
+                         enter the propagator (1D_FEM.c:65-66) */
   int nsteps;
   double ds;
   int rule;           /* SCFT_RULE_* */
@@ -131,13 +132,21 @@ typedef struct scft_solve_opts {
   int verify64;       /* FP32-converged instances are re-evaluated once in FP64 */
   int maxit;
   int depth;          /* Anderson history depth (<= 16) */
-  double beta;        /* mixing parameter */
+  double beta;        /* mixing parameter (initial 1 - lk of ADM_chen_C.c) */
   double clip;        /* max-norm bound on one field update */
   double grow;        /* restart the history when the error grows by this factor */
   double reg;         /* relative Tikhonov term of the least-squares solve */
   int residual_mode;  /* SCFT_MIX_LINEAR (phi - f0) or SCFT_MIX_LOG (ln phi - ln f0) */
   double precond;     /* a in (1 - a d2/dx2) applied to the mixing residual */
   int iters_per_graph;/* iterations captured in one CUDA graph */
+  int beta_schedule;  /* 1: the mixing parameter follows ADM_chen_C.c:125-129 (lk = 1 - beta is
+                         multiplied by 1 - beta once ||phi - f0|| < 0.03 after 100 iterations and
+                         reset below 1e-5); 0: fixed */
+  int weighted;       /* 1: the least squares and the clip weight node i by f0_i / max f0, the
+                         scale on which ||phi - f0||_inf is judged; 0: unweighted */
+  double step_cap;    /* one update moves no node by more than step_cap / ds (0: no cap) */
+  double field_floor; /* the field stays >= -field_floor / ds, so 1 + ds w >= 1 - field_floor
+                         (0: no floor) */
 } scft_solve_opts;
 
 typedef struct scft_result {
@@ -153,7 +162,8 @@ void scft_solve_opts_init(scft_solve_opts *o);
 
 /* Copies the instances to the device.  Returns SCFT_OK and *out, or an error. */
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out);
-/* Overwrite all fields (concatenated n_nodes values per instance). */
+/* Overwrite all fields (concatenated n_nodes values per instance; wall values
+   are kept for the free energy, the propagator ignores them). */
 int scft_batch_set_fields(scft_batch *b, const double *w_nodes);
 /* One propagator pass at the current fields (density and Q for every instance). */
 int scft_batch_evaluate(scft_batch *b, int precision);
@@ -166,6 +176,11 @@ int scft_batch_reset(scft_batch *b);
 /* Device time of the last scft_batch_evaluate / scft_batch_solve / scft_batch_reset,
    measured with CUDA events on the batch's stream (ms). */
 double scft_batch_last_ms(scft_batch *b);
+/* Progress of the last scft_batch_solve: after each CUDA-graph launch
+   (iters_per_graph iterations) the number of unfinished instances and the host
+   time since the solve started (ms).  Writes at most max entries and returns
+   the number of graph launches. */
+int scft_batch_trace(scft_batch *b, int max, int *active, double *ms);
 /* Per shape class of precision p: nodes per thread, warps per instance, instance
    count, algorithmic half-contour bytes of one pass (write + read of slices
    0..nsteps/2 of every node, 4 or 8 bytes each) and the event-timed duration (ms)
@@ -173,6 +188,13 @@ double scft_batch_last_ms(scft_batch *b);
    returns the number of classes (or an error code). */
 int scft_batch_profile(scft_batch *b, int precision, int max_classes, int *C, int *NW, int *items,
                        double *bytes, double *ms);
+/* Mean-field free energy of every instance at its current field, as
+   DEALII_SCFT/src/scft.cc:404-450 reports it:
+     F = ( int w_h f0 dx / f0bar / L + ln f0bar ) / (-1000),  f0bar = (1/L) int f0 dx,
+   with both integrals by Romberg (romint.c:21) over m+1 uniform samples of the
+   target on [0, L] (m a power of two >= 16; scft.cc uses 2^18) and w_h the
+   piecewise-linear field.  f0_samples: count x (m+1) doubles; F: count doubles. */
+int scft_batch_free_energy(scft_batch *b, int m, const double *f0_samples, double *F);
 /* Per-instance status bits of the last evaluate/solve (count ints). */
 int scft_batch_status(scft_batch *b, int *status);
 /* Choose the propagator shape of one instance: C nodes per thread (1,2,4,8) and
@@ -213,8 +235,9 @@ int scft_ws_batch_features(scft_batch *b, float *features, float *targets);
 /* Append the instances of b selected by mask (NULL: all) with their current
    fields as training samples.  Returns the dataset size or an error code. */
 int scft_ws_dataset_from_batch(scft_ws *ws, scft_batch *b, const int *mask);
-/* Adam on the dataset: steps minibatches of `batch` samples; losses (steps
-   floats, may be NULL) receives the minibatch losses. */
+/* Adam on the dataset: steps minibatches of `batch` samples, learning rate
+   decaying from lr to lr/50 on a cosine; losses (steps floats, may be NULL)
+   receives the minibatch losses. */
 int scft_ws_train(scft_ws *ws, int steps, int batch, float lr, unsigned long long seed, float *losses);
 /* Overwrite every field of b with the network's prediction (on b's stream;
    scft_batch_last_ms reports its device time). */

@@ -62,12 +62,13 @@ class Problem(C.Structure):
 class MixOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("beta", C.c_double), ("clip", C.c_double), ("grow", C.c_double),
                 ("reg", C.c_double), ("precond", C.c_double), ("maxit", C.c_int), ("depth", C.c_int),
-                ("mode", C.c_int)]
+                ("mode", C.c_int), ("schedule", C.c_int), ("cap", C.c_double), ("floor", C.c_double),
+                ("weighted", C.c_int)]
 
 
 # the batched GPU solver's defaults (scft_solve_opts_init)
 MIX_DEFAULTS = dict(tol=1e-6, beta=0.1, clip=1.0, grow=10.0, reg=1e-12, precond=1.0 / 6.0, maxit=2000,
-                    depth=10, mode=1)
+                    depth=10, mode=1, schedule=1, cap=0.25, floor=0.5, weighted=1)
 
 
 def _ptr(a: np.ndarray):

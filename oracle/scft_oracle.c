@@ -998,6 +998,12 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
   double *hdx = wprev + N, *hdg = hdx + (size_t)D * N, *G = hdg + (size_t)D * N;
   int cnt = 0, head = 0, rc = 1, it;
   double best = INFINITY, e = INFINITY;
+  const double lmd = 1.0 - o->beta;
+  double lk = lmd;
+  double fmx = 0.0;
+  for (int j = 0; j < N; j++) fmx = fmax(fmx, p->f0[j + 1]);
+  const double winv = (o->weighted && fmx > 0.0) ? 1.0 / fmx : 0.0;
+  const double wfloor = o->floor > 0.0 ? -o->floor / p->ds : -INFINITY;
   w[0] = w[n - 1] = 0.0;
   for (it = 0;; it++) {
     if (or_propagate(p, w, phi, NULL, NULL)) { rc = -3; break; }
@@ -1032,8 +1038,9 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
         const double *ds_ = hdg + (size_t)slot[t] * N;
         double sb = 0.0, sg = 0.0;
         for (int j = 0; j < N; j++) {
-          sb += ds_[j] * graw[j];
-          if (push) sg += hdg[(size_t)h * N + j] * ds_[j];
+          const double wj = o->weighted ? p->f0[j + 1] * winv : 1.0, w2 = wj * wj;
+          sb += ds_[j] * (graw[j] * w2);
+          if (push) sg += (hdg[(size_t)h * N + j] * w2) * ds_[j];
         }
         gam[t] = sb;
         if (push) { G[h * D + slot[t]] = sg; G[slot[t] * D + h] = sg; }
@@ -1053,21 +1060,30 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
       for (int t = 0; t < cnt; t++) rb -= gam[t] * hdg[(size_t)slot[t] * N + j];
       g[j] = rb;
     }
-    double dm = 0.0;
+    double dm = 0.0, da = 0.0;
     for (int j = 0; j < N; j++) {
-      double gc = g[j], gm = j > 0 ? g[j - 1] : 0.0, gp = j < N - 1 ? g[j + 1] : 0.0;
-      double a1 = p->x[j + 1] - p->x[j], a2 = p->x[j + 2] - p->x[j + 1];
-      double step = o->beta * (gc + o->precond * ((gc - gm) / a1 + (gc - gp) / a2) / (0.5 * (a1 + a2)));
+      double gc = g[j], lap = 0.0;
+      if (j > 0 && j < N - 1) {
+        double a1 = p->x[j + 1] - p->x[j], a2 = p->x[j + 2] - p->x[j + 1];
+        lap = ((gc - g[j - 1]) / a1 + (gc - g[j + 1]) / a2) / (0.5 * (a1 + a2));
+      }
+      double step = (1.0 - lk) * (gc + o->precond * lap);
       for (int t = 0; t < cnt; t++) step -= gam[t] * hdx[(size_t)slot[t] * N + j];
       wprev[j] = step;
-      dm = fmax(dm, fabs(step));
+      dm = fmax(dm, fabs(step) * (o->weighted ? p->f0[j + 1] * winv : 1.0));
+      da = fmax(da, fabs(step));
     }
     double scale = dm > o->clip ? o->clip / dm : 1.0;
+    if (o->cap > 0.0 && da * scale * p->ds > o->cap) scale = o->cap / (da * p->ds);
     for (int j = 0; j < N; j++) {
       double step = wprev[j];
       wprev[j] = w[j + 1];
       gprev[j] = graw[j];
-      w[j + 1] += scale * step;
+      w[j + 1] = fmax(w[j + 1] + scale * step, wfloor);
+    }
+    if (o->schedule) {
+      if (e < 0.03 && it > 100) lk *= lmd;
+      if (lk < 1e-5) lk = lmd;
     }
   }
   if (iters) *iters = it;

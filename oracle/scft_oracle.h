@@ -97,13 +97,19 @@ int or_broydn(or_vecfunc f, void *ctx, double *x, int n, double tol, int *iters,
 /* Safeguarded Anderson solve of one instance, the CPU restatement of the GPU
    batched solver's mixing (scft_gb300/csrc/mixing.cu, mix_kernel): mixing
    residual g = P(ln phi - ln f0) (mode 1) or P(phi - f0) (mode 0) with
-   P = 1 + a (-d2/dx2) (lumped FEM Laplacian), difference-form history of depth
-   <= 16, Tikhonov-regularised least squares, max-norm step clip and a history
-   restart when the error grows by `grow`.  w: full nodal field in/out.
+   P = 1 + a (-d2/dx2) (lumped FEM Laplacian, no curvature term at the first and
+   last interior nodes), difference-form history of depth <= 16,
+   Tikhonov-regularised least squares (inner products weighted by
+   (f0 / max f0)^2 when `weighted`), a step clip in the (f0 / max f0)-weighted
+   max norm, a cap of cap/ds on any node's change, a floor -floor/ds on the
+   field and a history restart when the error grows by `grow`.  w: full nodal
+   field in/out.
    Returns 0 converged (||phi - f0||_inf <= tol), 1 max iterations, 2 non-finite. */
 typedef struct or_mix_opts {
   double tol, beta, clip, grow, reg, precond;
-  int maxit, depth, mode;
+  int maxit, depth, mode, schedule; /* schedule: beta = 1 - lk with lk of ADM_chen_C.c:125-129 */
+  double cap, floor;                /* 0 disables either */
+  int weighted;
 } or_mix_opts;
 int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int *iters, double *err);
 

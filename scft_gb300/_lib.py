@@ -50,7 +50,9 @@ class ScftSolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("tol", C.c_double), ("tol32_factor", C.c_double),
                 ("verify64", C.c_int), ("maxit", C.c_int), ("depth", C.c_int), ("beta", C.c_double),
                 ("clip", C.c_double), ("grow", C.c_double), ("reg", C.c_double),
-                ("residual_mode", C.c_int), ("precond", C.c_double), ("iters_per_graph", C.c_int)]
+                ("residual_mode", C.c_int), ("precond", C.c_double), ("iters_per_graph", C.c_int),
+                ("beta_schedule", C.c_int), ("weighted", C.c_int), ("step_cap", C.c_double),
+                ("field_floor", C.c_double)]
 
 
 class ScftResult(C.Structure):
@@ -84,6 +86,8 @@ SIGNATURES = {
     "scft_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "scft_batch_reset": (C.c_int, [C.c_void_p]),
     "scft_batch_last_ms": (C.c_double, [C.c_void_p]),
+    "scft_batch_trace": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
+    "scft_batch_free_energy": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "scft_batch_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int), _dp, _dp]),
     "scft_batch_set_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),

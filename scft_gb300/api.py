@@ -237,6 +237,23 @@ class Batch:
         """Event-timed device duration of the last evaluate / solve / reset."""
         return float(self.lib.scft_batch_last_ms(self.h))
 
+    def free_energy(self, f0_samples):
+        """Free energy of each instance (scft.cc:404-450) from its target sampled
+        at m+1 uniform points of [0, L] (array count x (m+1), m a power of two)."""
+        fs = np.ascontiguousarray(f0_samples, dtype=np.float64)
+        m = fs.shape[1] - 1
+        F = np.empty(self.count)
+        check(self.lib.scft_batch_free_energy(self.h, int(m), _dp(fs), _dp(F)), "scft_batch_free_energy")
+        return F
+
+    def trace(self, max_entries=100000):
+        """(unfinished instances, ms since start) after each graph launch of the last solve."""
+        a = (C.c_int * max_entries)()
+        m = (C.c_double * max_entries)()
+        k = check(self.lib.scft_batch_trace(self.h, max_entries, a, m), "scft_batch_trace")
+        k = min(k, max_entries)
+        return np.array(a[:k]), np.array(m[:k])
+
     def profile(self, precision=L.F32, max_classes=64):
         """Per shape class: (C, NW, items, algorithmic bytes, ms) of one pass alone."""
         n = max_classes

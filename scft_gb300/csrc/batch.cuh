@@ -38,8 +38,11 @@ struct scft_batch {
   int depth = 0;
   double *d_graw = nullptr, *d_gcur = nullptr, *d_gprev = nullptr, *d_wprev = nullptr;
   double *d_hdx = nullptr, *d_hdg = nullptr, *d_gram = nullptr, *d_err = nullptr, *d_best = nullptr;
+  double *d_lk = nullptr;
   int *d_iters = nullptr, *d_hcount = nullptr, *d_hhead = nullptr, *d_nactive = nullptr;
   int *h_nactive = nullptr;
+  std::vector<int> trace_active;   // unfinished instances after each graph launch of the last solve
+  std::vector<double> trace_ms;    // host time since the solve started at that point
   cudaStream_t st = nullptr;
   std::vector<cudaStream_t> side;
   cudaEvent_t ev_fork = nullptr;

@@ -91,6 +91,13 @@ __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
   }
   e = block_max(e, sm);
   badv = block_max(badv, sm);
+  // weights f0_j / max f0: the scale on which ||phi - f0||_inf is judged
+  double fmx = 0.0;
+  if (m.weighted) {
+    for (int j = tid; j < N; j += MIX_THREADS) fmx = fmax(fmx, f0[j + 1]);
+    fmx = block_max(fmx, sm);
+  }
+  const double winv = (m.weighted && fmx > 0.0) ? 1.0 / fmx : 0.0;
   const int it = m.iters[inst];
   if (badv != 0.0) {
     if (tid == 0) { m.status[inst] |= ST_NONFINITE; m.active[inst] = 0; m.err[inst] = e; }
@@ -133,14 +140,17 @@ __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
   }
   __syncthreads();
   // 3. least squares on the raw mixing residual r: new Gram row <dr_h, dr_s>
-  //    and right-hand side <dr_s, r>
+  //    and right-hand side <dr_s, r>, inner products weighted by (f0_j / max f0)^2
+  //    so that nodes whose ||phi - f0|| is far below any tolerance (the walls)
+  //    do not steer the extrapolation
   if (cnt > 0) {
     double pb[MAXD], pg[MAXD];
 #pragma unroll
     for (int t = 0; t < MAXD; t++) { pb[t] = 0.0; pg[t] = 0.0; }
     for (int j = tid; j < N; j += MIX_THREADS) {
-      const double gv = graw[j];
-      const double dh = push ? hdg[(long long)h * N + j] : 0.0;
+      const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
+      const double gv = graw[j] * wj * wj;
+      const double dh = push ? hdg[(long long)h * N + j] * wj * wj : 0.0;
 #pragma unroll
       for (int t = 0; t < MAXD; t++) {
         if (t < cnt) {
@@ -185,34 +195,53 @@ __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
     gcur[j] = rb;
   }
   __syncthreads();
-  // 5. update w <- w - sum_s gam_s dx_s + beta (1 + a (-d2/dx2)) rbar, clipped in max norm
+  // 5. update w <- w - sum_s gam_s dx_s + beta (1 + a (-d2/dx2)) rbar
   //    (the preconditioner acts on the step only, so FP32 rounding noise it
-  //    amplifies never enters the least squares)
-  double dm = 0.0;
+  //    amplifies never enters the least squares; the mixed residual is
+  //    extended linearly past the first and last interior nodes, i.e. no
+  //    curvature term there); beta = 1 - lk.  The step is scaled so that its
+  //    f0-weighted max norm is <= clip and no node moves by more than
+  //    step_cap / ds; the field is kept >= -field_floor / ds.
+  const double beta = 1.0 - m.lk[inst];
+  const double dsi = m.ds[inst];
+  double dm = 0.0, da = 0.0;
   for (int j = tid; j < N; j += MIX_THREADS) {
     const double gc = gcur[j];
-    const double gm = (j > 0) ? gcur[j - 1] : 0.0, gp = (j < N - 1) ? gcur[j + 1] : 0.0;
-    const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
-    const double lap = ((gc - gm) / a1 + (gc - gp) / a2) / (0.5 * (a1 + a2));
-    double d = m.beta * (gc + m.precond * lap);
+    double lap = 0.0;
+    if (j > 0 && j < N - 1) {
+      const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
+      lap = ((gc - gcur[j - 1]) / a1 + (gc - gcur[j + 1]) / a2) / (0.5 * (a1 + a2));
+    }
+    double d = beta * (gc + m.precond * lap);
     for (int t = 0; t < cnt; t++) d -= gam[t] * hdx[(long long)sh_slot[t] * N + j];
     wprev[j] = d;  // staged; wprev receives the old field below
-    dm = fmax(dm, fabs(d));
+    const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
+    dm = fmax(dm, fabs(d) * wj);
+    da = fmax(da, fabs(d));
   }
   dm = block_max(dm, sm);
-  const double scale = (dm > m.clip) ? m.clip / dm : 1.0;
+  da = block_max(da, sm);
+  double scale = (dm > m.clip) ? m.clip / dm : 1.0;
+  if (m.step_cap > 0.0 && da * scale * dsi > m.step_cap) scale = m.step_cap / (da * dsi);
+  const double wfloor = (m.field_floor > 0.0) ? -m.field_floor / dsi : -INFINITY;
   for (int j = tid; j < N; j += MIX_THREADS) {
     const double wo = w[j + 1];
     const double d = wprev[j];
     wprev[j] = wo;
     gprev[j] = graw[j];
-    w[j + 1] = wo + scale * d;
+    w[j + 1] = fmax(wo + scale * d, wfloor);
   }
   if (tid == 0) {
     m.iters[inst] = it + 1;
     m.hcount[inst] = cnt;
     m.hhead[inst] = sh_ctl[1];
     m.err[inst] = e;
+    if (m.lk_schedule) {
+      double l = m.lk[inst];
+      if (e < 0.03 && it > 100) l *= m.lmd;
+      if (l < 1e-5) l = m.lmd;
+      m.lk[inst] = l;
+    }
   }
 }
 

@@ -19,6 +19,7 @@ struct MixDev {
   int *iters;
   double *err;     // ||phi - f0||_inf of the last evaluation
   double *best;    // best error since the last restart
+  double *lk;      // per instance: 1 - mixing parameter (ADM_chen_C.c:42, 122)
   double *graw, *gcur, *gprev, *wprev;  // interior vectors: residual, mixed residual, previous residual / field
   double *hdx, *hdg;                    // history of field / residual differences
   double *gram;                         // depth*depth per instance
@@ -27,7 +28,12 @@ struct MixDev {
   int maxit;
   int mode;        // 0: mixing residual phi - f0; 1: ln phi - ln f0
   int verify64;    // FP32-converged instances are re-evaluated once in FP64
-  double tol, tol32, beta, clip, grow, precond, reg;
+  int lk_schedule; // ADM_chen_C.c:125-129: lk *= lmd once err < 0.03 after 100 iterations, reset below 1e-5
+  double tol, tol32, lmd, clip, grow, precond, reg;
+  const double *ds;   // contour step per instance
+  int weighted;       // least squares and clip weighted by f0 / max f0
+  double step_cap;    // |step_i| <= step_cap / ds (0: off)
+  double field_floor; // w_i >= -field_floor / ds (0: off)
 };
 
 cudaError_t mix_launch(const MixDev &m, cudaStream_t st);

@@ -77,7 +77,7 @@ template <typename R, int C, int NW, bool DELTA>
 struct Propagator {
   static constexpr int T = 32 * NW;
   static constexpr int TC = T * C;
-  static constexpr int GPC = (T >= 256) ? 1 : 256 / T;  // groups per CTA
+  static constexpr int GPC = (T >= 64) ? 1 : 64 / T;    // groups per CTA (small CTAs: occupancy is register-bound)
   static constexpr int CTA = T * GPC;
   static constexpr int L2 = Log2<NW>::v;
   static constexpr int CI = (C > 1) ? C - 1 : 1;       // chunk-interior array extent
@@ -222,9 +222,11 @@ struct Propagator {
     R ibw;
     double vw, ww;
     {
-      double a = (lane == 0 || lane == 31) ? 0.0 : al;
-      double bb = (lane == 31) ? 1.0 : be;
-      double c = (lane >= 30) ? 0.0 : ga;
+      // NW == 1: the 32 chunk separators form one self-contained system (no
+      // coupling outside the warp), solved directly by PCR over all lanes.
+      double a = (lane == 0 || (NW > 1 && lane == 31)) ? 0.0 : al;
+      double bb = (NW > 1 && lane == 31) ? 1.0 : be;
+      double c = (NW > 1 ? lane >= 30 : lane == 31) ? 0.0 : ga;
       double k1d[5], k2d[5];
 #pragma unroll
       for (int l = 0; l < 5; l++) {
@@ -252,8 +254,8 @@ struct Propagator {
         rv = rv - k1d[l] * vm - k2d[l] * vp;
         rw = rw - k1d[l] * wm - k2d[l] * wp;
       }
-      vw = (lane == 31) ? 0.0 : rv * ibwd;
-      ww = (lane == 31) ? 0.0 : rw * ibwd;
+      vw = (NW == 1 || lane == 31) ? 0.0 : rv * ibwd;
+      ww = (NW == 1 || lane == 31) ? 0.0 : rw * ibwd;
     }
     // level 2: warp separators
     const double vw30 = __shfl_sync(FULL, vw, 30), ww30 = __shfl_sync(FULL, ww, 30);
@@ -306,8 +308,10 @@ struct Propagator {
     }
     R qLh = (P * C - 1 >= 0 && P * C - 1 < N) ? (R)1 : (R)0, qLl = (R)0;
     R qRh = ((P + 1) * C < N) ? (R)1 : (R)0, qRl = (R)0;
+    // padded unknowns (P*C + c >= N) are never stored or read back
 #pragma unroll
-    for (int c = 0; c < C; c++) slot[(long long)c * T + P] = qh[c];
+    for (int c = 0; c < C; c++)
+      if (P * C + c < N) slot[(long long)c * T + P] = qh[c];
     const R wend = S.qw[15];
 
     // ---------------- contour loop ----------------
@@ -326,7 +330,7 @@ struct Propagator {
         } else {
           const R *src = slot + (long long)(ns - k) * TC + P;
 #pragma unroll
-          for (int c = 0; c < C; c++) pre[c] = src[(long long)c * T];
+          for (int c = 0; c < C; c++) pre[c] = (P * C + c < N) ? src[(long long)c * T] : (R)0;
         }
       }
       // prefetch for step k+1: its slice ns-k-1 must have been stored at a step < k
@@ -334,7 +338,7 @@ struct Propagator {
       if (have_nxt) {
         const R *src = slot + (long long)(ns - k - 1) * TC + P;
 #pragma unroll
-        for (int c = 0; c < C; c++) nxt[c] = src[(long long)c * T];
+        for (int c = 0; c < C; c++) nxt[c] = (P * C + c < N) ? src[(long long)c * T] : (R)0;
       }
       // right-hand side
       R r[C];
@@ -367,17 +371,24 @@ struct Propagator {
       R zc0n = __shfl_down_sync(FULL, zc[0], 1);
       // chunk-separator right-hand side and warp-interior PCR
       R rho = (C > 1) ? fmaR(-r_dus, zc0n, fmaR(-r_dls, zc[C > 1 ? C - 2 : 0], r[C - 1])) : r[0];
-      R t = (lane == 31) ? (R)0 : rho;
+      R t = (NW == 1 || lane != 31) ? rho : (R)0;
 #pragma unroll
       for (int l = 0; l < 5; l++) {
         const int s = 1 << l;
         const R tm = __shfl_up_sync(FULL, t, s), tp = __shfl_down_sync(FULL, t, s);
         t = fmaR(-K2[l], tp, fmaR(-K1[l], tm, t));
       }
-      const R zw = t * ibw;
-      const R zw30 = __shfl_sync(FULL, zw, 30);
-      R Sprevw, Sown, Snextw, zwn = (R)0;
-      if (NW > 1) {
+      R Sp, Sprev, Snext;
+      if constexpr (NW == 1) {
+        Sp = t * ibw;
+        Sprev = __shfl_up_sync(FULL, Sp, 1);
+        Snext = __shfl_down_sync(FULL, Sp, 1);
+        if (lane == 0) Sprev = (R)0;
+        if (lane == 31) Snext = (R)0;
+      } else {
+        const R zw = t * ibw;
+        const R zw30 = __shfl_sync(FULL, zw, 30);
+        R zwn = (R)0;
         if (lane == 0) { S.pub_zc0[wid] = zc[0]; S.pub_zw[wid] = zw; }
         gsync(bar_id);
         if (lane == 31) {
@@ -399,23 +410,18 @@ struct Propagator {
           t2 = fmaR(-K2b[l], tp, fmaR(-K1b[l], tm, t2));
         }
         const R sw = t2 * iB2;
-        Sown = __shfl_sync(FULL, sw, wid);
-        Sprevw = __shfl_sync(FULL, sw, wid > 0 ? wid - 1 : 0);
-        Snextw = __shfl_sync(FULL, sw, wid + 1 < NW ? wid + 1 : wid);
+        const R Sown = __shfl_sync(FULL, sw, wid);
+        R Sprevw = __shfl_sync(FULL, sw, wid > 0 ? wid - 1 : 0);
+        R Snextw = __shfl_sync(FULL, sw, wid + 1 < NW ? wid + 1 : wid);
         if (wid == 0) Sprevw = (R)0;
         if (wid + 1 >= NW) Snextw = (R)0;
-      } else {
-        const R Rw = fmaR(-r_al, zw30, rho);
-        Sown = __shfl_sync(FULL, Rw * iB2, 31);
-        Sprevw = (R)0;
-        Snextw = (R)0;
+        // separator values and their neighbours
+        Sp = (lane == 31) ? Sown : fmaR(-r_ww, Sown, fmaR(-r_vw, Sprevw, zw));
+        Sprev = __shfl_up_sync(FULL, Sp, 1);
+        Snext = __shfl_down_sync(FULL, Sp, 1);
+        if (lane == 0) Sprev = Sprevw;
+        if (lane == 31) Snext = (wid + 1 < NW) ? fmaR(-r_wwn, Snextw, fmaR(-r_vwn, Sown, zwn)) : (R)0;
       }
-      // separator values and their neighbours
-      const R Sp = (lane == 31) ? Sown : fmaR(-r_ww, Sown, fmaR(-r_vw, Sprevw, zw));
-      R Sprev = __shfl_up_sync(FULL, Sp, 1);
-      R Snext = __shfl_down_sync(FULL, Sp, 1);
-      if (lane == 0) Sprev = Sprevw;
-      if (lane == 31) Snext = (NW > 1 && wid + 1 < NW) ? fmaR(-r_wwn, Snextw, fmaR(-r_vwn, Sown, zwn)) : (R)0;
       // chunk unknowns
       R xv[C];
 #pragma unroll
@@ -439,7 +445,8 @@ struct Propagator {
       if (k <= half) {
         R *dst = slot + (long long)k * TC + P;
 #pragma unroll
-        for (int c = 0; c < C; c++) dst[(long long)c * T] = qh[c];
+        for (int c = 0; c < C; c++)
+          if (P * C + c < N) dst[(long long)c * T] = qh[c];
       }
       if (acc_step) {
         R wk = (k == ns) ? wend : S.qw[min(__ffs(k) - 1, 14)];

@@ -45,12 +45,12 @@ static cudaError_t dispatch(int prec, int C, int NW, const BatchDev &b, const Cl
 int propagate_cta_threads(int C, int NW) {
   (void)C;
   const int T = 32 * NW;
-  return T >= 256 ? T : 256;
+  return T >= 64 ? T : 64;
 }
 int propagate_groups_per_cta(int C, int NW) {
   (void)C;
   const int T = 32 * NW;
-  return T >= 256 ? 1 : 256 / T;
+  return T >= 64 ? 1 : 64 / T;
 }
 bool propagate_has_class(int prec, int C, int NW) {
   bool ex = false;
@@ -380,7 +380,7 @@ static int fill_double(double *a, long long n, double v, cudaStream_t st) {
 
 static void free_mix(scft_batch *B) {
   dfree(B->d_graw); dfree(B->d_gcur); dfree(B->d_gprev); dfree(B->d_wprev);
-  dfree(B->d_hdx); dfree(B->d_hdg); dfree(B->d_gram); dfree(B->d_err); dfree(B->d_best);
+  dfree(B->d_hdx); dfree(B->d_hdg); dfree(B->d_gram); dfree(B->d_err); dfree(B->d_best); dfree(B->d_lk);
   dfree(B->d_iters); dfree(B->d_hcount); dfree(B->d_hhead); dfree(B->d_nactive);
   if (B->h_nactive) cudaFreeHost(B->h_nactive);
   B->h_nactive = nullptr;
@@ -395,7 +395,7 @@ static int ensure_mix(scft_batch *B, int depth) {
   if ((rc = dalloc(&B->d_graw, ni)) || (rc = dalloc(&B->d_gcur, ni)) || (rc = dalloc(&B->d_gprev, ni)) ||
       (rc = dalloc(&B->d_wprev, ni)) || (rc = dalloc(&B->d_hdx, ni * depth)) ||
       (rc = dalloc(&B->d_hdg, ni * depth)) || (rc = dalloc(&B->d_gram, c * depth * depth)) ||
-      (rc = dalloc(&B->d_err, c)) || (rc = dalloc(&B->d_best, c)) || (rc = dalloc(&B->d_iters, c)) ||
+      (rc = dalloc(&B->d_err, c)) || (rc = dalloc(&B->d_best, c)) || (rc = dalloc(&B->d_lk, c)) || (rc = dalloc(&B->d_iters, c)) ||
       (rc = dalloc(&B->d_hcount, c)) || (rc = dalloc(&B->d_hhead, c)) || (rc = dalloc(&B->d_nactive, 1)))
     return rc;
   CK(cudaMallocHost(&B->h_nactive, sizeof(int)));
@@ -469,8 +469,6 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
       hw[B->node_off[i] + k] = s.w0 ? s.w0[k] : 0.0;
     }
     if (!s.x) x[s.n_nodes - 1] = s.L;
-    hw[B->node_off[i]] = 0.0;
-    hw[B->node_off[i] + s.n_nodes - 1] = 0.0;
     quad_table(s.nsteps, s.ds, s.rule, hqw.data() + 16 * (size_t)i);
   }
   int rc;
@@ -532,7 +530,8 @@ static int evaluate(scft_batch *B, int p) {
 
 static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   const int p = o->precision;
-  if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0))
+  if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
+      !(o->beta > 0.0 && o->beta <= 1.0))
     return set_err(SCFT_EINVAL, "solve options");
   int rc = plan(B, p, 1.0);
   if (rc) return rc;
@@ -549,6 +548,7 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   CK(cudaMemsetAsync(B->d_hhead, 0, c * sizeof(int), st));
   CK(cudaMemsetAsync(B->d_gram, 0, (size_t)c * o->depth * o->depth * sizeof(double), st));
   if ((rc = fill_double(B->d_best, c, INFINITY, st))) return rc;
+  if ((rc = fill_double(B->d_lk, c, 1.0 - o->beta, st))) return rc;
   if ((rc = fill_double(B->d_err, c, INFINITY, st))) return rc;
 
   MixDev m;
@@ -558,12 +558,14 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   m.int_off = B->d_int_off;
   m.x = B->d_x; m.f0 = B->d_f0; m.phi = B->d_phi; m.w = B->d_w;
   m.active = B->d_active; m.status = B->d_status; m.iters = B->d_iters; m.err = B->d_err; m.best = B->d_best;
+  m.lk = B->d_lk; m.lk_schedule = o->beta_schedule; m.lmd = 1.0 - o->beta;
   m.graw = B->d_graw; m.gcur = B->d_gcur; m.gprev = B->d_gprev; m.wprev = B->d_wprev;
   m.hdx = B->d_hdx; m.hdg = B->d_hdg; m.gram = B->d_gram;
   m.hcount = B->d_hcount; m.hhead = B->d_hhead;
   m.depth = o->depth; m.maxit = o->maxit; m.mode = o->residual_mode; m.verify64 = verify ? 1 : 0;
-  m.tol = o->tol; m.tol32 = o->tol * o->tol32_factor; m.beta = o->beta; m.clip = o->clip;
+  m.tol = o->tol; m.tol32 = o->tol * o->tol32_factor; m.clip = o->clip;
   m.grow = o->grow; m.precond = o->precond; m.reg = o->reg;
+  m.ds = B->d_ds; m.weighted = o->weighted; m.step_cap = o->step_cap; m.field_floor = o->field_floor;
 
   const int K = std::max(1, o->iters_per_graph);
   // capture K iterations: propagate (FP32 and/or FP64 classes), mix; then count
@@ -597,11 +599,16 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   CK(ec);
   const long long max_launch = (long long)o->maxit / K + 3;
   int result = SCFT_OK;
+  B->trace_active.clear();
+  B->trace_ms.clear();
+  const auto t_start = std::chrono::steady_clock::now();
   for (long long L = 0;; L++) {
     cudaError_t e = cudaGraphLaunch(gexec, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { result = set_err(SCFT_ECUDA, "solver graph: %s", cudaGetErrorString(e)); break; }
     g_launches += per_graph;
+    B->trace_active.push_back(*B->h_nactive);
+    B->trace_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
     if (*B->h_nactive == 0) break;
     if (L + 1 >= max_launch) {
       // watchdog: the mixing kernel stops every instance at maxit, so this is a backstop
@@ -1270,6 +1277,10 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->residual_mode = SCFT_MIX_LOG;
   o->precond = 1.0 / 6.0;
   o->iters_per_graph = 8;
+  o->beta_schedule = 1;
+  o->weighted = 1;
+  o->step_cap = 0.25;
+  o->field_floor = 0.5;
 }
 
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {
@@ -1278,9 +1289,7 @@ int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {
 
 int scft_batch_set_fields(scft_batch *b, const double *w_nodes) {
   if (!b || !w_nodes) return set_err(SCFT_EINVAL, "scft_batch_set_fields");
-  std::vector<double> w(w_nodes, w_nodes + b->total_nodes);
-  for (int i = 0; i < b->count; i++) { w[b->node_off[i]] = 0.0; w[b->node_off[i] + b->n[i] - 1] = 0.0; }
-  CK(cudaMemcpy(b->d_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_w, w_nodes, b->total_nodes * sizeof(double), cudaMemcpyHostToDevice));
   return SCFT_OK;
 }
 
@@ -1338,6 +1347,16 @@ int scft_batch_reset(scft_batch *b) {
 }
 
 double scft_batch_last_ms(scft_batch *b) { return b ? (double)b->last_ms : -1.0; }
+
+int scft_batch_trace(scft_batch *b, int max, int *active, double *ms) {
+  if (!b || max < 0) return set_err(SCFT_EINVAL, "scft_batch_trace");
+  const int n = (int)b->trace_active.size();
+  for (int i = 0; i < n && i < max; i++) {
+    if (active) active[i] = b->trace_active[i];
+    if (ms) ms[i] = b->trace_ms[i];
+  }
+  return n;
+}
 
 int scft_batch_profile(scft_batch *b, int precision, int max_classes, int *C, int *NW, int *items,
                        double *bytes, double *ms) {

@@ -550,8 +550,10 @@ int scft_ws_train(scft_ws *W, int steps, int batch, float lr, unsigned long long
     if ((rc = ws_forward(W, batch)) || (rc = ws_backward(W, batch, s))) { cudaFreeHost(h_idx); return rc; }
     W->adam_t++;
     const float c1 = 1.f - std::pow(b1, (float)W->adam_t), c2 = 1.f - std::pow(b2, (float)W->adam_t);
-    adam_kernel<<<(W->nparam + 255) / 256, 256, 0, W->st>>>(W->d_p, W->d_g, W->d_m, W->d_v, W->nparam, lr, b1, b2,
-                                                            1e-8f, c1, c2);
+    // cosine decay from lr to lr/50 over the run
+    const float lr_s = lr * (0.02f + 0.49f * (1.f + std::cos(3.14159265f * (float)s / (float)steps)));
+    adam_kernel<<<(W->nparam + 255) / 256, 256, 0, W->st>>>(W->d_p, W->d_g, W->d_m, W->d_v, W->nparam, lr_s, b1,
+                                                            b2, 1e-8f, c1, c2);
     scft_count_launches(1);
     WCK(cudaGetLastError());
   }

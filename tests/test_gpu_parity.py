@@ -142,3 +142,18 @@ def test_lost_dominance_is_flagged():
     w[0] = w[-1] = 0
     _, _, st = gpu_eval([dict(d, w0=w)], F64)
     assert st[0] & 1
+
+
+def test_free_energy_known_answer(oracle):
+    """N=33_for_read.txt stores the mean-field free energy 0.001945037280931 of
+    its field (scft.cc:404-450: Romberg over 2^18+1 samples of the tanh^2 target)."""
+    g = json.load(open(os.path.join(GOLD, "dealii_N33.json")))
+    x, w = np.array(g["x"]), np.array(g["w"])
+    m = 2 ** 18
+    xs = np.linspace(0.0, g["L"], m + 1)
+    fs = oracle.f0_tanh2_le(xs, g["tau"])
+    d = {"n_nodes": len(x), "x": x, "L": g["L"], "f0": np.array(g["f0"]), "w0": w, "nsteps": 2048,
+         "ds": 1.0 / 2048}
+    with api.Batch([d]) as b:
+        F = b.free_energy(fs[None, :])
+    assert abs(F[0] - g["file_free_energy"]) < 1e-13
