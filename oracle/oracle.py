@@ -152,6 +152,20 @@ class Oracle:
         f = np.ascontiguousarray(f, dtype=np.float64)
         return self.L.or_romint(_ptr(f), m, hh)
 
+    def free_energy(self, x, w, f0_samples):
+        """Mean-field free energy reported by DEALII_SCFT/src/scft.cc:404-450:
+        F = (<w f0> / <f0> + ln <f0>) / (-1000), <.> the Romberg average
+        (romint.c:21-57) over m+1 uniform samples of [x_0, x_L], w the
+        piecewise-linear field of the mesh."""
+        x = np.asarray(x, dtype=np.float64)
+        fs = np.ascontiguousarray(f0_samples, dtype=np.float64)
+        m = len(fs) - 1
+        xs = x[0] + ((x[-1] - x[0]) * np.arange(m + 1, dtype=np.float64)) / m
+        wq = np.interp(xs, x, np.asarray(w, dtype=np.float64))
+        a = self.romint(wq * fs, m, 1.0 / m)
+        b = self.romint(fs, m, 1.0 / m)
+        return (a / b + np.log(b)) / -1000.0
+
     def quad_weights(self, nsteps, ds, rule):
         W = np.empty(nsteps + 1)
         if self.L.or_quad_weights(nsteps, ds, rule, _ptr(W)):

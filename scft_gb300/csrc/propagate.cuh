@@ -29,6 +29,8 @@
 // Kahan-compensated.
 // FP64 path (DELTA = false): the direct form D q' = M q of the reference.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace scft {
@@ -107,6 +109,196 @@ struct Propagator {
       const int inst = cls.items[item];
       if (b.active[inst] != cls.want) continue;
       instance(b, S, P, lane, wid, inst, slot, bar_id);
+    }
+  }
+
+  // Contour loop of the FP32 increment form on packed pairs (sm_100+ f32x2
+  // arithmetic).  Pair i of a thread holds its chunk unknowns i and i + C/2, so
+  // the neighbour pairs of pair i are pairs i - 1 and i + 1 except at the two
+  // ends, where one lane comes from the neighbouring chunk's shadow value.
+  //   * increments are added to the (hi, lo) pair by the fast two-sum
+  //     (s = hi + d, lo += d - (s - hi)); every 16 steps the pair is
+  //     renormalised (hi = hi + lo, lo = the rounding error of that sum);
+  //   * slices of the first half are stored as float2 pairs, [step][pair][thread];
+  //   * the density terms are summed in FP32 over blocks of 16 steps, and each
+  //     block sum enters the Kahan-compensated total.
+  // The neighbour shadows (qLh/qLl, qRh/qRl) receive the same operations in the
+  // same order as the values they mirror, so they stay bit-identical.
+  template <typename SepF>
+  __device__ static __forceinline__ void contour_f32x2(
+      GroupSmem<R, NW> &S, int P, int N, int ns, int half, R *slot, bool last_chunk, R wend,
+      const R (&cl)[C], const R (&cd)[C], const R (&cu)[C], const R (&ka)[C], const R (&kb)[C],
+      const R (&mm)[CI], const R (&ib)[CI], const R (&ub)[CI], const R (&vc)[CI], const R (&wc)[CI],
+      R r_vcn, R r_wcn, SepF &separators, R (&qh)[C], R (&ql)[C], R &qLh, R &qLl, R &qRh, R &qRl,
+      R (&acc)[C], R (&cmp)[C]) {
+    constexpr int H = C / 2;
+    auto sub2 = [](float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); };
+    auto mk = [](float a, float b) { return make_float2(a, b); };
+    float2 cl2[H], cd2[H], cu2[H], nka2[H], nkb2[H], ib2[H], nvc2[H], nwc2[H];
+    float nmm[C], nub[C];
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+      const int u = i + H;  // second node of the pair
+      cl2[i] = mk(cl[i], cl[u]);
+      cd2[i] = mk(cd[i], cd[u]);
+      cu2[i] = mk(cu[i], cu[u]);
+      nka2[i] = mk(-ka[i], -ka[u]);
+      nkb2[i] = mk(-kb[i], -kb[u]);
+      // the separator (node C - 1) has no chunk-interior z: xv = Sp there
+      ib2[i] = mk(ib[i], (u < C - 1) ? ib[u < C - 1 ? u : 0] : 0.f);
+      nvc2[i] = mk(-vc[i], (u < C - 1) ? -vc[u < C - 1 ? u : 0] : 0.f);
+      nwc2[i] = mk(-wc[i], (u < C - 1) ? -wc[u < C - 1 ? u : 0] : 1.f);
+    }
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      nmm[c] = (c >= 1 && c < C - 1) ? -mm[c < C - 1 ? c : 0] : 0.f;
+      nub[c] = (c < C - 1) ? -ub[c < C - 1 ? c : 0] : 0.f;
+    }
+    float2 qh2[H], ql2[H], blk2[H], acc2[H], cmp2[H];
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+      qh2[i] = mk(qh[i], qh[i + H]);
+      ql2[i] = mk(0.f, 0.f);
+      blk2[i] = acc2[i] = cmp2[i] = mk(0.f, 0.f);
+    }
+    float2 *slot2 = reinterpret_cast<float2 *>(slot);
+    // a pair is stored and read back when its first node is a real unknown
+    auto live = [&](int i) { return P * C + i < N; };
+#pragma unroll
+    for (int i = 0; i < H; i++)
+      if (live(i)) slot2[(long long)i * T + P] = qh2[i];
+
+    // one implicit-Euler step: q += D^{-1} (-ds (K + W) q)
+    auto step = [&]() {
+      float2 r2[H];
+      {
+        const float2 lh = mk(qLh, qh2[H - 1].y), ll = mk(qLl, ql2[H - 1].y);
+        const float2 rh = mk(qh2[0].y, qRh), rl = mk(ql2[0].y, qRl);
+#pragma unroll
+        for (int i = 0; i < H; i++) {
+          const float2 Lh = (i == 0) ? lh : qh2[i > 0 ? i - 1 : 0];
+          const float2 Ll = (i == 0) ? ll : ql2[i > 0 ? i - 1 : 0];
+          const float2 Rh = (i == H - 1) ? rh : qh2[i < H - 1 ? i + 1 : 0];
+          const float2 Rl = (i == H - 1) ? rl : ql2[i < H - 1 ? i + 1 : 0];
+          float2 m = __fmul2_rn(cd2[i], qh2[i]);
+          m = __ffma2_rn(cl2[i], Lh, m);
+          m = __ffma2_rn(cu2[i], Rh, m);
+          const float2 d1 = __fadd2_rn(sub2(qh2[i], Lh), sub2(ql2[i], Ll));
+          const float2 d2 = __fadd2_rn(sub2(qh2[i], Rh), sub2(ql2[i], Rl));
+          r2[i] = __ffma2_rn(nka2[i], d1, __ffma2_rn(nkb2[i], d2, m));
+        }
+      }
+      // chunk-interior Thomas sweep (unknowns 0 .. C-2); y of the separator is 0
+      float y[C];
+      y[0] = r2[0].x;
+#pragma unroll
+      for (int c = 1; c < C; c++) {
+        const float rc = (c < H) ? r2[c < H ? c : 0].x : r2[c >= H ? c - H : 0].y;
+        y[c] = (c < C - 1) ? __fmaf_rn(nmm[c], y[c - 1], rc) : 0.f;
+      }
+      float2 z2[H];
+#pragma unroll
+      for (int i = 0; i < H; i++) z2[i] = __fmul2_rn(mk(y[i], y[i + H]), ib2[i]);
+      float z[C];
+#pragma unroll
+      for (int i = 0; i < H; i++) { z[i] = z2[i].x; z[i + H] = z2[i].y; }
+#pragma unroll
+      for (int c = C - 3; c >= 0; c--) z[c] = __fmaf_rn(nub[c], z[c + 1], z[c]);
+#pragma unroll
+      for (int i = 0; i < H; i++) z2[i] = mk(z[i], z[i + H]);
+      const float rlast = r2[H - 1].y;
+      float zc0n, Sp, Sprev, Snext;
+      separators(z[0], z[C - 2], rlast, zc0n, Sp, Sprev, Snext);
+      const float2 Sp2 = mk(Sp, Sp), Sq2 = mk(Sprev, Sprev);
+      const float dL = Sprev;
+      const float dR = last_chunk ? 0.f : __fmaf_rn(-r_wcn, Snext, __fmaf_rn(-r_vcn, Sp, zc0n));
+#pragma unroll
+      for (int i = 0; i < H; i++) {
+        const float2 xv = __ffma2_rn(nwc2[i], Sp2, __ffma2_rn(nvc2[i], Sq2, z2[i]));
+        const float2 sum = __fadd2_rn(qh2[i], xv);
+        ql2[i] = __fadd2_rn(ql2[i], sub2(xv, sub2(sum, qh2[i])));
+        qh2[i] = sum;
+      }
+      {
+        const float s1 = __fadd_rn(qLh, dL);
+        qLl = __fadd_rn(qLl, __fsub_rn(dL, __fsub_rn(s1, qLh)));
+        qLh = s1;
+        const float s2 = __fadd_rn(qRh, dR);
+        qRl = __fadd_rn(qRl, __fsub_rn(dR, __fsub_rn(s2, qRh)));
+        qRh = s2;
+      }
+    };
+    auto renorm = [&]() {
+#pragma unroll
+      for (int i = 0; i < H; i++) {
+        const float2 h = __fadd2_rn(qh2[i], ql2[i]);
+        ql2[i] = sub2(ql2[i], sub2(h, qh2[i]));
+        qh2[i] = h;
+      }
+      float h = __fadd_rn(qLh, qLl);
+      qLl = __fsub_rn(qLl, __fsub_rn(h, qLh));
+      qLh = h;
+      h = __fadd_rn(qRh, qRl);
+      qRl = __fsub_rn(qRl, __fsub_rn(h, qRh));
+      qRh = h;
+    };
+    auto flush = [&]() {
+#pragma unroll
+      for (int i = 0; i < H; i++) {
+        const float2 yv = sub2(blk2[i], cmp2[i]);
+        const float2 tt = __fadd2_rn(acc2[i], yv);
+        cmp2[i] = sub2(sub2(tt, acc2[i]), yv);
+        acc2[i] = tt;
+        blk2[i] = mk(0.f, 0.f);
+      }
+    };
+    auto weight = [&](int k) { return (k == ns) ? wend : S.qw[min(__ffs(k) - 1, 14)]; };
+
+    // first half: store slices 1..half (the middle slice pairs with itself when ns is even)
+    for (int k = 1; k <= half; k++) {
+      step();
+      if ((k & 15) == 0) renorm();
+      float2 *dst = slot2 + (long long)k * H * T + P;
+#pragma unroll
+      for (int i = 0; i < H; i++)
+        if (live(i)) dst[(long long)i * T] = qh2[i];
+      if (k == ns - k) {
+        const float wk = weight(k);
+#pragma unroll
+        for (int i = 0; i < H; i++) blk2[i] = __ffma2_rn(__fmul2_rn(mk(wk, wk), qh2[i]), qh2[i], blk2[i]);
+      }
+    }
+    // second half: slice k pairs with the stored slice ns - k (prefetched one step ahead)
+    float2 nxt2[H];
+    {
+      const float2 *src = slot2 + (long long)(ns - half - 1) * H * T + P;
+#pragma unroll
+      for (int i = 0; i < H; i++) nxt2[i] = live(i) ? src[(long long)i * T] : mk(0.f, 0.f);
+    }
+    int nblk = 0;
+    for (int k = half + 1; k <= ns; k++) {
+      float2 pre2[H];
+#pragma unroll
+      for (int i = 0; i < H; i++) pre2[i] = nxt2[i];
+      if (k < ns) {
+        const float2 *src = slot2 + (long long)(ns - k - 1) * H * T + P;
+#pragma unroll
+        for (int i = 0; i < H; i++) nxt2[i] = live(i) ? src[(long long)i * T] : mk(0.f, 0.f);
+      }
+      step();
+      if ((k & 15) == 0) renorm();
+      const float w2 = 2.f * weight(k);
+#pragma unroll
+      for (int i = 0; i < H; i++) blk2[i] = __ffma2_rn(__fmul2_rn(mk(w2, w2), qh2[i]), pre2[i], blk2[i]);
+      if (++nblk == 16) { flush(); nblk = 0; }
+    }
+    flush();
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+      qh[i] = qh2[i].x; qh[i + H] = qh2[i].y;
+      ql[i] = ql2[i].x; ql[i + H] = ql2[i].y;
+      acc[i] = acc2[i].x; acc[i + H] = acc2[i].y;
+      cmp[i] = cmp2[i].x; cmp[i + H] = cmp2[i].y;
     }
   }
 
@@ -298,6 +490,66 @@ struct Propagator {
     const R r_dls = (R)dls, r_dus = (R)dus, r_vcn = (R)vcn, r_wcn = (R)wcn;
     const bool last_chunk = (P == T - 1);
 
+    // Separator solve of one contour step.  In: this thread's chunk-local z at
+    // its first and last interior unknowns and the right-hand side at its
+    // separator (C == 1: the right-hand side).  Out: the next chunk's z at its
+    // first unknown, this thread's separator value and its neighbours'.
+    auto separators = [&](R zc0, R zcl, R rl, R &zc0n, R &Sp, R &Sprev, R &Snext) {
+      zc0n = __shfl_down_sync(FULL, zc0, 1);
+      // chunk-separator right-hand side and warp-interior PCR
+      R rho = (C > 1) ? fmaR(-r_dus, zc0n, fmaR(-r_dls, zcl, rl)) : rl;
+      R t = (NW == 1 || lane != 31) ? rho : (R)0;
+#pragma unroll
+      for (int l = 0; l < 5; l++) {
+        const int s = 1 << l;
+        const R tm = __shfl_up_sync(FULL, t, s), tp = __shfl_down_sync(FULL, t, s);
+        t = fmaR(-K2[l], tp, fmaR(-K1[l], tm, t));
+      }
+      if constexpr (NW == 1) {
+        Sp = t * ibw;
+        Sprev = __shfl_up_sync(FULL, Sp, 1);
+        Snext = __shfl_down_sync(FULL, Sp, 1);
+        if (lane == 0) Sprev = (R)0;
+        if (lane == 31) Snext = (R)0;
+      } else {
+        const R zw = t * ibw;
+        const R zw30 = __shfl_sync(FULL, zw, 30);
+        R zwn = (R)0;
+        if (lane == 0) { S.pub_zc0[wid] = zc0; S.pub_zw[wid] = zw; }
+        gsync(bar_id);
+        if (lane == 31) {
+          const bool has_next = (wid + 1 < NW);
+          const R zcx = has_next ? S.pub_zc0[wid + 1] : (R)0;
+          zwn = has_next ? S.pub_zw[wid + 1] : (R)0;
+          if (C > 1) {
+            zc0n = zcx;
+            rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zcl, rl));
+          }
+          S.pub_R[wid] = fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho));
+        }
+        gsync(bar_id);
+        R t2 = (lane < NW) ? S.pub_R[lane] : (R)0;
+#pragma unroll
+        for (int l = 0; l < L2; l++) {
+          const int s = 1 << l;
+          const R tm = __shfl_up_sync(FULL, t2, s), tp = __shfl_down_sync(FULL, t2, s);
+          t2 = fmaR(-K2b[l], tp, fmaR(-K1b[l], tm, t2));
+        }
+        const R sw = t2 * iB2;
+        const R Sown = __shfl_sync(FULL, sw, wid);
+        R Sprevw = __shfl_sync(FULL, sw, wid > 0 ? wid - 1 : 0);
+        R Snextw = __shfl_sync(FULL, sw, wid + 1 < NW ? wid + 1 : wid);
+        if (wid == 0) Sprevw = (R)0;
+        if (wid + 1 >= NW) Snextw = (R)0;
+        // separator values and their neighbours
+        Sp = (lane == 31) ? Sown : fmaR(-r_ww, Sown, fmaR(-r_vw, Sprevw, zw));
+        Sprev = __shfl_up_sync(FULL, Sp, 1);
+        Snext = __shfl_down_sync(FULL, Sp, 1);
+        if (lane == 0) Sprev = Sprevw;
+        if (lane == 31) Snext = (wid + 1 < NW) ? fmaR(-r_wwn, Snextw, fmaR(-r_vwn, Sown, zwn)) : (R)0;
+      }
+    };
+
     // ---------------- state ----------------
     R qh[C], ql[C], acc[C], cmp[C];
 #pragma unroll
@@ -308,11 +560,15 @@ struct Propagator {
     }
     R qLh = (P * C - 1 >= 0 && P * C - 1 < N) ? (R)1 : (R)0, qLl = (R)0;
     R qRh = ((P + 1) * C < N) ? (R)1 : (R)0, qRl = (R)0;
+    const R wend = S.qw[15];
+    if constexpr (DELTA && C >= 2 && std::is_same<R, float>::value) {
+      contour_f32x2(S, P, N, ns, half, slot, last_chunk, wend, cl, cd, cu, ka, kb, mm, ib, ub, vc, wc,
+                    r_vcn, r_wcn, separators, qh, ql, qLh, qLl, qRh, qRl, acc, cmp);
+    } else {
     // padded unknowns (P*C + c >= N) are never stored or read back
 #pragma unroll
     for (int c = 0; c < C; c++)
       if (P * C + c < N) slot[(long long)c * T + P] = qh[c];
-    const R wend = S.qw[15];
 
     // ---------------- contour loop ----------------
     // The slice read back at step k (ns - k) is prefetched during step k-1
@@ -368,60 +624,8 @@ struct Propagator {
       } else {
         zc[0] = (R)0;
       }
-      R zc0n = __shfl_down_sync(FULL, zc[0], 1);
-      // chunk-separator right-hand side and warp-interior PCR
-      R rho = (C > 1) ? fmaR(-r_dus, zc0n, fmaR(-r_dls, zc[C > 1 ? C - 2 : 0], r[C - 1])) : r[0];
-      R t = (NW == 1 || lane != 31) ? rho : (R)0;
-#pragma unroll
-      for (int l = 0; l < 5; l++) {
-        const int s = 1 << l;
-        const R tm = __shfl_up_sync(FULL, t, s), tp = __shfl_down_sync(FULL, t, s);
-        t = fmaR(-K2[l], tp, fmaR(-K1[l], tm, t));
-      }
-      R Sp, Sprev, Snext;
-      if constexpr (NW == 1) {
-        Sp = t * ibw;
-        Sprev = __shfl_up_sync(FULL, Sp, 1);
-        Snext = __shfl_down_sync(FULL, Sp, 1);
-        if (lane == 0) Sprev = (R)0;
-        if (lane == 31) Snext = (R)0;
-      } else {
-        const R zw = t * ibw;
-        const R zw30 = __shfl_sync(FULL, zw, 30);
-        R zwn = (R)0;
-        if (lane == 0) { S.pub_zc0[wid] = zc[0]; S.pub_zw[wid] = zw; }
-        gsync(bar_id);
-        if (lane == 31) {
-          const bool has_next = (wid + 1 < NW);
-          const R zcx = has_next ? S.pub_zc0[wid + 1] : (R)0;
-          zwn = has_next ? S.pub_zw[wid + 1] : (R)0;
-          if (C > 1) {
-            zc0n = zcx;
-            rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zc[C > 1 ? C - 2 : 0], r[C - 1]));
-          }
-          S.pub_R[wid] = fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho));
-        }
-        gsync(bar_id);
-        R t2 = (lane < NW) ? S.pub_R[lane] : (R)0;
-#pragma unroll
-        for (int l = 0; l < L2; l++) {
-          const int s = 1 << l;
-          const R tm = __shfl_up_sync(FULL, t2, s), tp = __shfl_down_sync(FULL, t2, s);
-          t2 = fmaR(-K2b[l], tp, fmaR(-K1b[l], tm, t2));
-        }
-        const R sw = t2 * iB2;
-        const R Sown = __shfl_sync(FULL, sw, wid);
-        R Sprevw = __shfl_sync(FULL, sw, wid > 0 ? wid - 1 : 0);
-        R Snextw = __shfl_sync(FULL, sw, wid + 1 < NW ? wid + 1 : wid);
-        if (wid == 0) Sprevw = (R)0;
-        if (wid + 1 >= NW) Snextw = (R)0;
-        // separator values and their neighbours
-        Sp = (lane == 31) ? Sown : fmaR(-r_ww, Sown, fmaR(-r_vw, Sprevw, zw));
-        Sprev = __shfl_up_sync(FULL, Sp, 1);
-        Snext = __shfl_down_sync(FULL, Sp, 1);
-        if (lane == 0) Sprev = Sprevw;
-        if (lane == 31) Snext = (wid + 1 < NW) ? fmaR(-r_wwn, Snextw, fmaR(-r_vwn, Sown, zwn)) : (R)0;
-      }
+      R zc0n, Sp, Sprev, Snext;
+      separators(zc[0], zc[C > 1 ? C - 2 : 0], (C > 1) ? r[C - 1] : r[0], zc0n, Sp, Sprev, Snext);
       // chunk unknowns
       R xv[C];
 #pragma unroll
@@ -467,6 +671,8 @@ struct Propagator {
       }
     }
 
+    }  // contour loop of the direct form / C == 1
+
     // ---------------- epilogue: phi, Q, status ----------------
     double qpart = 0.0;
     double *phi = b.phi + off;
@@ -503,7 +709,7 @@ struct Propagator {
 };
 
 template <typename R, int C, int NW, bool DELTA>
-__global__ void __launch_bounds__(Propagator<R, C, NW, DELTA>::CTA)
+__global__ void __launch_bounds__(Propagator<R, C, NW, DELTA>::CTA, 1)
 propagate_kernel(BatchDev b, ClassDev cls) {
   using Pp = Propagator<R, C, NW, DELTA>;
   __shared__ GroupSmem<R, NW> sm[Pp::GPC];

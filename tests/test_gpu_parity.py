@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as orc
-from scft_gb300 import F32, F64, RULE_ROMBERG, RULE_TRAPEZOID, api, workloads as W
+from scft_gb300 import F32, F64, RULE_ROMBERG, RULE_TRAPEZOID, ST_CONVERGED, api, workloads as W
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -157,3 +157,41 @@ def test_free_energy_known_answer(oracle):
     with api.Batch([d]) as b:
         F = b.free_energy(fs[None, :])
     assert abs(F[0] - g["file_free_energy"]) < 1e-13
+
+
+def test_free_energy_matches_oracle(oracle):
+    insts = W.batch_mixed(8, seed=21)
+    m = 2 ** 12
+    fs = np.stack([W.gauss_wall_f0(np.linspace(0.0, d["L"], m + 1), d["L"]) for d in insts])
+    ws = [field(d) for d in insts]
+    with api.Batch([dict(d, w0=w) for d, w in zip(insts, ws)]) as b:
+        F = b.free_energy(fs)
+    for i, d in enumerate(insts):
+        ref = oracle.free_energy(d["x"], ws[i], fs[i])
+        assert abs(F[i] - ref) <= 1e-12 * max(1.0, abs(ref)), (i, F[i], ref)
+
+
+def test_fp32_solution_error_single_large(oracle):
+    """1024 elements, 2048 steps, L = 4: the field converged by the batched
+    solver with the FP32 propagator against the oracle's FP64 solve of the same
+    instance (both to ||phi - f0||_inf <= 1e-6): density at the converged
+    fields, Q and the mean-field free energy."""
+    d = W.single_large()
+    p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d.get("rule", RULE_ROMBERG))
+    rc, w64, it64, err64 = oracle.anderson_solve(p, d["w0"], tol=1e-6)
+    assert rc == 0
+    phi64, Q64 = oracle.propagate(p, w64)
+    with api.Batch([d]) as b:
+        r = b.solve(api.solve_opts(precision=F32, tol=1e-6))
+        assert r["status"][0] & ST_CONVERGED
+        w32, phi32, Q32 = b.get()
+    m = 2 ** 14
+    xs = np.linspace(0.0, d["L"], m + 1)
+    fs = W.gauss_wall_f0(xs, d["L"])
+    F64 = oracle.free_energy(d["x"], w64, fs)
+    F32 = oracle.free_energy(d["x"], w32[0], fs)
+    e_phi = float(np.abs(phi32[0] - phi64).max())
+    e_Q = abs(Q32[0] - Q64) / abs(Q64)
+    e_F = abs(F32 - F64)
+    print(f"fp32 solution error: phi {e_phi:.3e} Q(rel) {e_Q:.3e} F {e_F:.3e} (F64 {F64:.15e})")
+    assert e_phi <= 3e-6 and e_Q <= 1e-5 and e_F <= 1e-8

@@ -62,6 +62,17 @@ def test_f0bar_known_answer(oracle):
     assert abs(fbar - load("res_m32.json")["mphi"]) < 1e-11
 
 
+def test_free_energy_known_answer(oracle):
+    """N=33_for_read.txt stores the mean-field free energy 0.001945037280931 of its
+    field (scft.cc:404-450: Romberg over 2^18+1 samples of the tanh^2 target)."""
+    g = load("dealii_N33.json")
+    m = 2 ** 18
+    xs = np.linspace(0.0, g["L"], m + 1)
+    fs = oracle.f0_tanh2_le(xs, g["tau"])
+    F = oracle.free_energy(np.array(g["x"]), np.array(g["w"]), fs)
+    assert abs(F - g["file_free_energy"]) < 1e-13
+
+
 def test_res_phi_column_is_the_target(oracle):
     """Exp_m32_n2048_IE.res: its phi column equals the tanh^2 wall profile."""
     g = load("res_m32.json")
