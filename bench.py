@@ -179,15 +179,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic(workload: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+def committed_traffic(workload: str, C: int, NW: int, alg_bytes: float):
+    """DRAM bytes per launch of the dominant kernel: the committed ncu summary
+    of this workload gives, per shape class, DRAM bytes (read + write) per
+    algorithmic byte measured on a smaller launch of the same class; scaled to
+    this launch by its algorithmic bytes."""
     path = os.path.join(ROOT, "profiles", f"propagate_f32_{workload}.md")
     if not os.path.exists(path):
         return None
+    key = f"dram_traffic_per_algorithmic_byte <float,{C},{NW}>:"
     for ln in open(path):
-        if ln.strip().startswith("dram_bytes_per_launch:"):
+        if ln.strip().startswith(key):
             try:
-                return float(ln.split(":", 1)[1].split()[0])
+                return float(ln.strip()[len(key):].split()[0]) * alg_bytes
             except ValueError:
                 return None
     return None
@@ -315,7 +319,7 @@ def ours_arm(args):
     dom = max(prof, key=lambda c: c["ms"])
     peak, peak_kind = peaks()
     achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
-    traffic = committed_traffic(args.workload)
+    traffic = committed_traffic(args.workload, dom["C"], dom["NW"], dom["bytes"])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_kind,
                 "kernel": f"propagate_kernel<float,C={dom['C']},NW={dom['NW']},increment form>",
@@ -340,6 +344,9 @@ def ours_arm(args):
                  if len(tr_ms) and (tr_active <= 0.1 * len(mine)).any() else None,
                  "ms_total_host": float(tr_ms[-1]) if len(tr_ms) else None},
         "converged_per_step": conv_all,
+        "status_last_step": {name: int(((r["status"] & bit) != 0).sum()) for name, bit in
+                             (("converged", 4), ("max_iterations", 8), ("non_finite", 2), ("not_dominant", 1),
+                              ("restarted", 16), ("watchdog", 32))},
         "clocks": clk,
         "roofline": roofline,
     }
@@ -353,7 +360,8 @@ def ours_arm(args):
         c64 = int(((r64["status"] & ST_CONVERGED) != 0).sum())
         line["batched_fp64_cold"] = {"value": c64 / (b.last_ms() / 1e3), "unit": UNIT, "ms": b.last_ms(),
                                      "converged": c64, "iterations_mean": float(r64["iterations"].mean())}
-        line["speedup_vs_batched_fp64_cold"] = value / line["batched_fp64_cold"]["value"]
+        line["speedup_vs_batched_fp64_cold"] = (value / line["batched_fp64_cold"]["value"]
+                                                if c64 else None)
         # the plain form: one instance per solve (no batching), FP64 propagator, cold start;
         # device time summed over a strided sample of the same batch
         sample = cpu_sample(mine, args.plain_sample)
@@ -369,13 +377,13 @@ def ours_arm(args):
             p_conv += int((r1["status"][0] & ST_CONVERGED) != 0)
             p_its.append(int(r1["iterations"][0]))
             s1.close()
-        line["plain_fp64"] = {"value": p_conv / (p_ms / 1e3), "unit": UNIT, "ms": p_ms, "converged": p_conv,
+        line["plain_fp64"] = {"value": p_conv / (p_ms / 1e3) if p_ms > 0 else 0.0, "unit": UNIT, "ms": p_ms, "converged": p_conv,
                               "iterations_mean": float(np.mean(p_its)),
                               "form": "one instance per solve (no batching), FP64 propagator, cold start, "
                                       "same Anderson mixing",
                               "sample": f"{len(sample)} of {len(mine)} instances, every "
                                         f"{max(1, len(mine) // args.plain_sample)}th"}
-        line["speedup_vs_plain_fp64"] = value / line["plain_fp64"]["value"]
+        line["speedup_vs_plain_fp64"] = value / line["plain_fp64"]["value"] if p_conv else None
     b.close()
 
     # end to end through the C ABI with host buffers

@@ -172,7 +172,7 @@ struct Propagator {
     auto step = [&]() {
       float2 r2[H];
       {
-        const float2 lh = mk(qLh, qh2[H - 1].y), ll = mk(qLl, ql2[H - 1].y);
+        const float2 lh = mk(qLh, qh2[H - 1].x), ll = mk(qLl, ql2[H - 1].x);
         const float2 rh = mk(qh2[0].y, qRh), rl = mk(ql2[0].y, qRl);
 #pragma unroll
         for (int i = 0; i < H; i++) {

@@ -188,10 +188,10 @@ def test_fp32_solution_error_single_large(oracle):
     m = 2 ** 14
     xs = np.linspace(0.0, d["L"], m + 1)
     fs = W.gauss_wall_f0(xs, d["L"])
-    F64 = oracle.free_energy(d["x"], w64, fs)
-    F32 = oracle.free_energy(d["x"], w32[0], fs)
+    fe64 = oracle.free_energy(d["x"], w64, fs)
+    fe32 = oracle.free_energy(d["x"], w32[0], fs)
     e_phi = float(np.abs(phi32[0] - phi64).max())
     e_Q = abs(Q32[0] - Q64) / abs(Q64)
-    e_F = abs(F32 - F64)
-    print(f"fp32 solution error: phi {e_phi:.3e} Q(rel) {e_Q:.3e} F {e_F:.3e} (F64 {F64:.15e})")
+    e_F = abs(fe32 - fe64)
+    print(f"fp32 solution error: phi {e_phi:.3e} Q(rel) {e_Q:.3e} F {e_F:.3e} (F64 {fe64:.15e})")
     assert e_phi <= 3e-6 and e_Q <= 1e-5 and e_F <= 1e-8
