@@ -188,6 +188,14 @@ int scft_batch_trace(scft_batch *b, int max, int *active, double *ms);
    returns the number of classes (or an error code). */
 int scft_batch_profile(scft_batch *b, int precision, int max_classes, int *C, int *NW, int *items,
                        double *bytes, double *ms);
+/* Propagator launches of the last scft_batch_solve, per shape class of the
+   given precision: launches that evaluated at least one instance, their
+   algorithmic bytes (write and read of every half-contour slice) and their
+   summed durations from CUDA events recorded around each launch inside the
+   solve graphs.  Returns the number of classes (entries written <= max_classes).
+   No reference counterpart (measurement). */
+int scft_batch_live_stats(scft_batch *b, int precision, int max_classes, int *C, int *NW, long long *launches,
+                          double *bytes, double *ms);
 /* Mean-field free energy of every instance at its current field, as
    DEALII_SCFT/src/scft.cc:404-450 reports it:
      F = ( int w_h f0 dx / f0bar / L + ln f0bar ) / (-1000),  f0bar = (1/L) int f0 dx,

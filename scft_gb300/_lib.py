@@ -32,6 +32,7 @@ MIX_LINEAR, MIX_LOG = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int)
 VECFUNC = C.CFUNCTYPE(None, C.c_int, _dp, _dp)
 
 
@@ -88,6 +89,7 @@ SIGNATURES = {
     "scft_batch_last_ms": (C.c_double, [C.c_void_p]),
     "scft_batch_trace": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
     "scft_batch_free_energy": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
+    "scft_batch_live_stats": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _ip, C.POINTER(C.c_longlong), _dp, _dp]),
     "scft_batch_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int), _dp, _dp]),
     "scft_batch_set_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),

@@ -263,6 +263,16 @@ class Batch:
                   "scft_batch_profile")
         return [dict(C=Cs[i], NW=NWs[i], items=its[i], bytes=by[i], ms=ms[i]) for i in range(min(k, n))]
 
+    def live_stats(self, precision=L.F32, max_classes=64):
+        """Per shape class, over the propagator launches of the last solve that
+        evaluated anything: (C, NW, launches, algorithmic bytes, summed ms)."""
+        n = max_classes
+        Cs, NWs = (C.c_int * n)(), (C.c_int * n)()
+        ln, by, ms = (C.c_longlong * n)(), (C.c_double * n)(), (C.c_double * n)()
+        k = check(self.lib.scft_batch_live_stats(self.h, int(precision), n, Cs, NWs, ln, by, ms),
+                  "scft_batch_live_stats")
+        return [dict(C=Cs[i], NW=NWs[i], launches=ln[i], bytes=by[i], ms=ms[i]) for i in range(min(k, n))]
+
     def set_shape(self, precision, index, C_nodes, NW):
         check(self.lib.scft_batch_set_shape(self.h, int(precision), int(index), int(C_nodes), int(NW)),
               "scft_batch_set_shape")

@@ -47,6 +47,14 @@ struct scft_batch {
   std::vector<cudaStream_t> side;
   cudaEvent_t ev_fork = nullptr;
   std::vector<cudaEvent_t> ev_join;
+  // Live statistics of the propagator launches inside the solve graphs: one
+  // event pair and one work counter per (iteration of the graph, precision,
+  // class); read after every replay, accumulated per class over one solve.
+  std::vector<cudaEvent_t> ev_live;
+  unsigned long long *d_work = nullptr, *h_work = nullptr;
+  int live_cap = 0, live_maxc = 0;
+  std::vector<double> live_ms[2], live_units[2];
+  std::vector<long long> live_launches[2];
 };
 
 

@@ -32,6 +32,7 @@ struct ClassDev {
   long long slot_elems;    // elements per worker slot
   int workers;             // number of slots
   int want;                // evaluate instances whose active flag equals this value
+  unsigned long long *work = nullptr;  // if set: += n (nsteps/2 + 1) per instance evaluated
 };
 
 // Status bits written by the kernels.

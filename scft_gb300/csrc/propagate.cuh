@@ -35,6 +35,17 @@
 
 namespace scft {
 
+// Packed FP32 path: the (hi, lo) pairs are renormalised every PACKED_RENORM
+// steps and density terms are summed in FP32 over PACKED_BLOCK steps before
+// entering the Kahan total (both powers of two; 1 and 1 reproduce the rounding
+// of a per-step two-sum and a per-step Kahan sum).
+#ifndef PACKED_RENORM
+#define PACKED_RENORM 1
+#endif
+#ifndef PACKED_BLOCK
+#define PACKED_BLOCK 1
+#endif
+
 template <typename R>
 __device__ __forceinline__ R fmaR(R a, R b, R c);
 template <>
@@ -109,6 +120,8 @@ struct Propagator {
       const int inst = cls.items[item];
       if (b.active[inst] != cls.want) continue;
       instance(b, S, P, lane, wid, inst, slot, bar_id);
+      if (cls.work && P == 0)
+        atomicAdd(cls.work, (unsigned long long)b.n[inst] * (unsigned long long)(b.nsteps[inst] / 2 + 1));
     }
   }
 
@@ -117,11 +130,11 @@ struct Propagator {
   // the neighbour pairs of pair i are pairs i - 1 and i + 1 except at the two
   // ends, where one lane comes from the neighbouring chunk's shadow value.
   //   * increments are added to the (hi, lo) pair by the fast two-sum
-  //     (s = hi + d, lo += d - (s - hi)); every 16 steps the pair is
+  //     (s = hi + d, lo += d - (s - hi)); every PACKED_RENORM steps the pair is
   //     renormalised (hi = hi + lo, lo = the rounding error of that sum);
   //   * slices of the first half are stored as float2 pairs, [step][pair][thread];
-  //   * the density terms are summed in FP32 over blocks of 16 steps, and each
-  //     block sum enters the Kahan-compensated total.
+  //   * the density terms are summed in FP32 over blocks of PACKED_BLOCK steps,
+  //     and each block sum enters the Kahan-compensated total.
   // The neighbour shadows (qLh/qLl, qRh/qRl) receive the same operations in the
   // same order as the values they mirror, so they stay bit-identical.
   template <typename SepF>
@@ -132,6 +145,7 @@ struct Propagator {
       R r_vcn, R r_wcn, SepF &separators, R (&qh)[C], R (&ql)[C], R &qLh, R &qLl, R &qRh, R &qRl,
       R (&acc)[C], R (&cmp)[C]) {
     constexpr int H = C / 2;
+    constexpr int kRenorm = PACKED_RENORM, kBlock = PACKED_BLOCK;
     auto sub2 = [](float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); };
     auto mk = [](float a, float b) { return make_float2(a, b); };
     float2 cl2[H], cd2[H], cu2[H], nka2[H], nkb2[H], ib2[H], nvc2[H], nwc2[H];
@@ -257,7 +271,7 @@ struct Propagator {
     // first half: store slices 1..half (the middle slice pairs with itself when ns is even)
     for (int k = 1; k <= half; k++) {
       step();
-      if ((k & 15) == 0) renorm();
+      if ((k & (kRenorm - 1)) == 0) renorm();
       float2 *dst = slot2 + (long long)k * H * T + P;
 #pragma unroll
       for (int i = 0; i < H; i++)
@@ -286,11 +300,11 @@ struct Propagator {
         for (int i = 0; i < H; i++) nxt2[i] = live(i) ? src[(long long)i * T] : mk(0.f, 0.f);
       }
       step();
-      if ((k & 15) == 0) renorm();
+      if ((k & (kRenorm - 1)) == 0) renorm();
       const float w2 = 2.f * weight(k);
 #pragma unroll
       for (int i = 0; i < H; i++) blk2[i] = __ffma2_rn(__fmul2_rn(mk(w2, w2), qh2[i]), pre2[i], blk2[i]);
-      if (++nblk == 16) { flush(); nblk = 0; }
+      if (++nblk == kBlock) { flush(); nblk = 0; }
     }
     flush();
 #pragma unroll

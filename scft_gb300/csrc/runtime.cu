@@ -318,29 +318,86 @@ static void class_dev(const scft_batch *B, const ClassPlan &c, ClassDev *d) {
   d->want = c.prec == PREC_F32 ? 1 : 2;
 }
 
+// Index of the live-statistics slot of (iteration k of a graph, precision p, class i).
+static int live_index(const scft_batch *B, int k, int p, int i) { return (k * 2 + p) * B->live_maxc + i; }
+
 // Enqueue one propagator pass of precision p on B->st (forked over class streams).
-static int enqueue_propagate(scft_batch *B, int p) {
+// live_k >= 0 (inside a solve graph): each class launch is bracketed by external
+// event records on its stream and counts its work into the live slot.
+static int enqueue_propagate(scft_batch *B, int p, int live_k = -1) {
   auto &plans = B->plans[p];
   if (plans.empty()) return SCFT_OK;
   const BatchDev b = batch_dev(B);
   for (auto &c : plans) CK(cudaMemsetAsync(B->d_heads + c.head, 0, sizeof(int), B->st));
-  if (plans.size() == 1) {
-    ClassDev d;
-    class_dev(B, plans[0], &d);
-    CK(propagate_launch(p, plans[0].C, plans[0].NW, b, d, plans[0].grid, B->st));
-    g_launches++;
-    return SCFT_OK;
-  }
-  CK(cudaEventRecord(B->ev_fork, B->st));
-  for (size_t i = 0; i < plans.size(); i++) {
+  auto launch = [&](size_t i, cudaStream_t s) -> int {
     ClassDev d;
     class_dev(B, plans[i], &d);
-    CK(cudaStreamWaitEvent(B->side[i], B->ev_fork, 0));
-    CK(propagate_launch(p, plans[i].C, plans[i].NW, b, d, plans[i].grid, B->side[i]));
+    int li = -1;
+    if (live_k >= 0) {
+      li = live_index(B, live_k, p, (int)i);
+      d.work = B->d_work + li;
+      CK(cudaEventRecordWithFlags(B->ev_live[2 * li], s, cudaEventRecordExternal));
+    }
+    CK(propagate_launch(p, plans[i].C, plans[i].NW, b, d, plans[i].grid, s));
     g_launches++;
+    if (li >= 0) CK(cudaEventRecordWithFlags(B->ev_live[2 * li + 1], s, cudaEventRecordExternal));
+    return SCFT_OK;
+  };
+  if (plans.size() == 1) return launch(0, B->st);
+  CK(cudaEventRecord(B->ev_fork, B->st));
+  for (size_t i = 0; i < plans.size(); i++) {
+    CK(cudaStreamWaitEvent(B->side[i], B->ev_fork, 0));
+    int rc = launch(i, B->side[i]);
+    if (rc) return rc;
     CK(cudaEventRecord(B->ev_join[i], B->side[i]));
   }
   for (size_t i = 0; i < plans.size(); i++) CK(cudaStreamWaitEvent(B->st, B->ev_join[i], 0));
+  return SCFT_OK;
+}
+
+// Make room for the live statistics of K iterations per graph.
+static int live_prepare(scft_batch *B, int K) {
+  const int maxc = (int)std::max<size_t>(1, std::max(B->plans[0].size(), B->plans[1].size()));
+  const int need = K * 2 * maxc;
+  if (need > B->live_cap) {
+    if (B->d_work) cudaFree(B->d_work);
+    if (B->h_work) cudaFreeHost(B->h_work);
+    B->d_work = nullptr;
+    B->h_work = nullptr;
+    CK(cudaMalloc(&B->d_work, need * sizeof(unsigned long long)));
+    CK(cudaMallocHost(&B->h_work, need * sizeof(unsigned long long)));
+    while ((int)B->ev_live.size() < 2 * need) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      B->ev_live.push_back(e);
+    }
+    B->live_cap = need;
+  }
+  B->live_maxc = maxc;
+  for (int p = 0; p < 2; p++) {
+    B->live_ms[p].assign(B->plans[p].size(), 0.0);
+    B->live_units[p].assign(B->plans[p].size(), 0.0);
+    B->live_launches[p].assign(B->plans[p].size(), 0);
+  }
+  return SCFT_OK;
+}
+
+// After a replay: accumulate the launches of that replay that evaluated anything.
+static int live_collect(scft_batch *B, int K, bool f32, bool f64) {
+  for (int k = 0; k < K; k++)
+    for (int p = 0; p < 2; p++) {
+      if ((p == PREC_F32 && !f32) || (p == PREC_F64 && !f64)) continue;
+      for (size_t i = 0; i < B->plans[p].size(); i++) {
+        const int li = live_index(B, k, p, (int)i);
+        const unsigned long long u = B->h_work[li];
+        if (u == 0) continue;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, B->ev_live[2 * li], B->ev_live[2 * li + 1]));
+        B->live_ms[p][i] += ms;
+        B->live_units[p][i] += (double)u;
+        B->live_launches[p][i]++;
+      }
+    }
   return SCFT_OK;
 }
 
@@ -417,6 +474,9 @@ static void destroy_batch(scft_batch *B) {
   if (B->t1) cudaEventDestroy(B->t1);
   for (auto s : B->side) cudaStreamDestroy(s);
   for (auto e : B->ev_join) cudaEventDestroy(e);
+  for (auto e : B->ev_live) cudaEventDestroy(e);
+  if (B->d_work) cudaFree(B->d_work);
+  if (B->h_work) cudaFreeHost(B->h_work);
   if (B->ev_fork) cudaEventDestroy(B->ev_fork);
   if (B->st) cudaStreamDestroy(B->st);
   delete B;
@@ -572,12 +632,15 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   long long per_graph = 0;
+  if ((rc = live_prepare(B, K))) return rc;
+  const size_t live_bytes = (size_t)K * 2 * B->live_maxc * sizeof(unsigned long long);
   CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   long long before = g_launches.load();
   int crc = SCFT_OK;
+  if (cudaMemsetAsync(B->d_work, 0, live_bytes, st) != cudaSuccess) crc = set_err(SCFT_ECUDA, "live reset");
   for (int k = 0; k < K && !crc; k++) {
-    if (p == PREC_F32) crc = enqueue_propagate(B, PREC_F32);
-    if (!crc && (p == PREC_F64 || verify)) crc = enqueue_propagate(B, PREC_F64);
+    if (p == PREC_F32) crc = enqueue_propagate(B, PREC_F32, k);
+    if (!crc && (p == PREC_F64 || verify)) crc = enqueue_propagate(B, PREC_F64, k);
     if (!crc) {
       cudaError_t e = mix_launch(m, st);
       g_launches++;
@@ -588,6 +651,7 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
     count_active_kernel<<<1, 256, 0, st>>>(B->d_active, c, B->d_nactive);
     g_launches++;
     cudaMemcpyAsync(B->h_nactive, B->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(B->h_work, B->d_work, live_bytes, cudaMemcpyDeviceToHost, st);
   }
   per_graph = g_launches.load() - before;
   g_launches -= per_graph;  // counted again per replay below
@@ -607,6 +671,7 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { result = set_err(SCFT_ECUDA, "solver graph: %s", cudaGetErrorString(e)); break; }
     g_launches += per_graph;
+    if ((rc = live_collect(B, K, p == PREC_F32, p == PREC_F64 || verify))) { result = rc; break; }
     B->trace_active.push_back(*B->h_nactive);
     B->trace_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
     if (*B->h_nactive == 0) break;
@@ -1388,6 +1453,22 @@ int scft_batch_profile(scft_batch *b, int precision, int max_classes, int *C, in
     if (ms) ms[k] = t;
   }
   return (int)plans.size();
+}
+
+int scft_batch_live_stats(scft_batch *b, int precision, int max_classes, int *C, int *NW, long long *launches,
+                          double *bytes, double *ms) {
+  if (!b || (precision != 0 && precision != 1) || max_classes < 0) return set_err(SCFT_EINVAL, "scft_batch_live_stats");
+  const auto &plans = b->plans[precision];
+  const double esz = precision == PREC_F32 ? 4.0 : 8.0;
+  const size_t nc = std::min(plans.size(), b->live_ms[precision].size());
+  for (size_t k = 0; k < nc && (int)k < max_classes; k++) {
+    if (C) C[k] = plans[k].C;
+    if (NW) NW[k] = plans[k].NW;
+    if (launches) launches[k] = b->live_launches[precision][k];
+    if (bytes) bytes[k] = 2.0 * esz * b->live_units[precision][k];
+    if (ms) ms[k] = b->live_ms[precision][k];
+  }
+  return (int)nc;
 }
 
 int scft_batch_destroy(scft_batch *b) {

@@ -159,3 +159,18 @@ def test_batched_solver_converges_like_oracle(oracle):
         assert np.abs(oracle_residual(oracle, d, w[i])).max() <= 1e-6 * (1 + 1e-6)
         its.append(it)
     assert abs(r["iterations"].mean() - np.mean(its)) <= 0.25 * np.mean(its)
+
+
+def test_live_stats_count_the_solve():
+    """Every propagator launch inside the solve graphs that evaluated anything is
+    timed by its event pair and counted: the first iteration alone evaluates
+    every instance once."""
+    insts = W.batch_mixed(24, seed=31)
+    with api.Batch(insts) as b:
+        r = b.solve(api.solve_opts(precision=F32, tol=1e-6))
+        st = b.live_stats(F32)
+    one_pass = sum(2.0 * 4 * d["n_nodes"] * (d["nsteps"] // 2 + 1) for d in insts)
+    assert sum(c["bytes"] for c in st) >= one_pass
+    assert all(c["ms"] > 0 for c in st if c["launches"])
+    assert max(c["launches"] for c in st) >= 1
+    assert max(c["launches"] for c in st) <= int(r["iterations"].max()) + 1
