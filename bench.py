@@ -344,7 +344,7 @@ def ours_arm(args):
                    "start": ("learned warm start (conv net, weights " + os.path.relpath(args.weights, ROOT) + ")")
                    if ws is not None else "cold (w0 ~ U[-0.1, 0.1])",
                    "l2": "working set (half-contour stores of concurrent instances) larger than L2",
-                   "mixing": "Anderson depth 10, beta 0.1, ln-residual with (1 - d2/dx2 / 6) preconditioner",
+                   "mixing": "Anderson depth 10, beta 1.0, ln-residual with (1 - 0.6 d2/dx2) preconditioner",
                    "parallelism": f"replicas x{world}, batch split by cost"},
         "gpu_launches": launches,
         "iterations_mean": statistics.mean(iters),
@@ -455,7 +455,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="warmstart_eval")
     ap.add_argument("--count", type=int, default=None)
-    ap.add_argument("--cpu-sample", type=int, default=192)
+    ap.add_argument("--cpu-sample", type=int, default=1536)
     ap.add_argument("--plain-sample", type=int, default=48, help="instances solved one at a time for the plain form")
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--cold", action="store_true", help="ignore the warm-start weights")

@@ -147,6 +147,10 @@ typedef struct scft_solve_opts {
   double step_cap;    /* one update moves no node by more than step_cap / ds (0: no cap) */
   double field_floor; /* the field stays >= -field_floor / ds, so 1 + ds w >= 1 - field_floor
                          (0: no floor) */
+  int fused;          /* 1: each instance iterates on its own inside one persistent launch per shape
+                         class (contour pass and Anderson step by the same thread group, no barrier
+                         across the batch; FP32 without verify64); 0: every iteration is a batch-wide
+                         step (propagator launches, then the mixing kernel) replayed from CUDA graphs */
 } scft_solve_opts;
 
 typedef struct scft_result {

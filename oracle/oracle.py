@@ -67,8 +67,8 @@ class MixOpts(C.Structure):
 
 
 # the batched GPU solver's defaults (scft_solve_opts_init)
-MIX_DEFAULTS = dict(tol=1e-6, beta=0.1, clip=1.0, grow=10.0, reg=1e-12, precond=1.0 / 6.0, maxit=2000,
-                    depth=10, mode=1, schedule=1, cap=0.25, floor=0.5, weighted=1)
+MIX_DEFAULTS = dict(tol=1e-6, beta=1.0, clip=1.0, grow=10.0, reg=1e-12, precond=0.6, maxit=2000,
+                    depth=10, mode=1, schedule=0, cap=0.25, floor=0.5, weighted=1)
 
 
 def _ptr(a: np.ndarray):

@@ -53,7 +53,7 @@ class ScftSolveOpts(C.Structure):
                 ("clip", C.c_double), ("grow", C.c_double), ("reg", C.c_double),
                 ("residual_mode", C.c_int), ("precond", C.c_double), ("iters_per_graph", C.c_int),
                 ("beta_schedule", C.c_int), ("weighted", C.c_int), ("step_cap", C.c_double),
-                ("field_floor", C.c_double)]
+                ("field_floor", C.c_double), ("fused", C.c_int)]
 
 
 class ScftResult(C.Structure):

@@ -1,0 +1,256 @@
+// mix_group.cuh -- one batched Anderson iteration of one instance, carried out
+// by a group of 32*NW threads (FP64).  Used by the one-CTA-per-instance
+// mix_kernel (NW = 8, __syncthreads) and by the fused solve kernels, where the
+// propagator's own group runs the update between two contour passes (named
+// barrier).
+//
+// The step: residual check, difference-form history of the mixing residual,
+// weighted regularised least squares, a preconditioned and clipped step,
+// restart safeguard (the safeguarded form of adm.c:24-313 / ADM_chen_C.c:18-147
+// used by the batched solver; the CPU restatement is or_anderson_solve in the
+// oracle).
+#pragma once
+#include "mixing.cuh"
+
+namespace scft {
+
+constexpr int MIX_MAXD = 16;
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int s = 16; s > 0; s >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, s));
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+  return v;
+}
+
+// Solve the k x k system A g = b (row-major, A overwritten) by Gaussian
+// elimination with partial pivoting; single thread.
+__device__ inline void small_solve(double *A, double *b, int k) {
+  for (int c = 0; c < k; c++) {
+    int p = c;
+    double big = fabs(A[c * k + c]);
+    for (int r = c + 1; r < k; r++)
+      if (fabs(A[r * k + c]) > big) { big = fabs(A[r * k + c]); p = r; }
+    if (p != c) {
+      for (int j = 0; j < k; j++) { double t = A[c * k + j]; A[c * k + j] = A[p * k + j]; A[p * k + j] = t; }
+      double t = b[c]; b[c] = b[p]; b[p] = t;
+    }
+    double piv = A[c * k + c];
+    if (piv == 0.0) piv = 1e-300;
+    for (int r = c + 1; r < k; r++) {
+      double f = A[r * k + c] / piv;
+      for (int j = c; j < k; j++) A[r * k + j] -= f * A[c * k + j];
+      b[r] -= f * b[c];
+    }
+  }
+  for (int c = k - 1; c >= 0; c--) {
+    double s = b[c];
+    for (int j = c + 1; j < k; j++) s -= A[c * k + j] * b[j];
+    double piv = A[c * k + c];
+    b[c] = s / (piv == 0.0 ? 1e-300 : piv);
+  }
+}
+
+// Shared memory of one group's mixing step.
+template <int NW>
+struct MixSmem {
+  double sm[NW];
+  double red[2 * MIX_MAXD][NW];
+  double gam[MIX_MAXD];
+  int slot[MIX_MAXD];
+  int ctl[4];
+};
+
+// Group-wide max of v (every thread of the group receives it).
+template <int NW, typename Sync>
+__device__ __forceinline__ double group_max(double v, MixSmem<NW> &S, int tid, Sync &sync) {
+  const int lane = tid & 31, wid = tid >> 5;
+  v = warp_max(v);
+  sync();
+  if (lane == 0) S.sm[wid] = v;
+  sync();
+  double r = (lane < NW) ? S.sm[lane] : 0.0;
+  return warp_max(r);
+}
+
+// One Anderson iteration of instance `inst` by threads tid = 0 .. 32*NW-1 of a
+// group; `sync` is the group's barrier.  Returns true (in every thread) when the
+// instance is finished: converged (or handed to the FP64 check), non-finite, or
+// at the iteration limit.  On false the field m.w of the instance holds the next
+// iterate.
+template <int NW, typename Sync>
+__device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Sync &sync) {
+  constexpr int NT = 32 * NW;
+  const int lane = tid & 31, wid = tid >> 5;
+  const int act = m.active[inst];
+  const int n = m.n[inst], N = n - 2;
+  const long long no = m.node_off[inst], io = m.int_off[inst];
+  const double *x = m.x + no, *f0 = m.f0 + no, *phi = m.phi + no;
+  double *w = m.w + no;
+  double *graw = m.graw + io, *gcur = m.gcur + io, *gprev = m.gprev + io, *wprev = m.wprev + io;
+  const int D = m.depth;
+  double *hdx = m.hdx + io * D, *hdg = m.hdg + io * D;
+  double *G = m.gram + (long long)inst * D * D;
+
+  // 1. residual, its norm, raw mixing residual
+  double e = 0.0, badv = 0.0;
+  for (int j = tid; j < N; j += NT) {
+    // L2 loads: in the fused solve phi was written by other threads of this kernel
+    const double p = __ldcg(phi + j + 1), f = f0[j + 1], r = p - f;
+    if (!isfinite(r)) badv = 1.0;
+    e = fmax(e, fabs(r));
+    graw[j] = m.mode ? (log(fmax(p, 1e-300)) - log(f)) : r;
+  }
+  e = group_max(e, S, tid, sync);
+  badv = group_max(badv, S, tid, sync);
+  // weights f0_j / max f0: the scale on which ||phi - f0||_inf is judged
+  double fmx = 0.0;
+  if (m.weighted) {
+    for (int j = tid; j < N; j += NT) fmx = fmax(fmx, f0[j + 1]);
+    fmx = group_max(fmx, S, tid, sync);
+  }
+  const double winv = (m.weighted && fmx > 0.0) ? 1.0 / fmx : 0.0;
+  const int it = m.iters[inst];
+  if (badv != 0.0) {
+    if (tid == 0) { m.status[inst] |= ST_NONFINITE; m.active[inst] = 0; m.err[inst] = e; }
+    return true;
+  }
+  const double tol_here = (act == 1) ? m.tol32 : m.tol;
+  if (e <= tol_here) {
+    if (tid == 0) {
+      m.err[inst] = e;
+      if (act == 1 && m.verify64) m.active[inst] = 2;
+      else { m.status[inst] |= ST_CONVERGED; m.active[inst] = 0; }
+    }
+    return true;
+  }
+  if (it >= m.maxit) {
+    if (tid == 0) { m.status[inst] |= ST_MAXIT; m.active[inst] = 0; m.err[inst] = e; }
+    return true;
+  }
+  // 2. history bookkeeping (restart when the error grew by more than `grow`)
+  if (tid == 0) {
+    int cnt = m.hcount[inst], head = m.hhead[inst];
+    double best = m.best[inst];
+    const bool restart = (it > 0) && (e > m.grow * best);
+    if (restart) { cnt = 0; best = e; m.status[inst] |= ST_RESTARTED; }
+    else best = (it == 0) ? e : fmin(best, e);
+    const int push = (it > 0) && !restart;
+    const int h = head;
+    if (push) { head = (head + 1) % D; cnt = cnt + 1 < D ? cnt + 1 : D; }
+    for (int t = 0; t < cnt; t++) S.slot[t] = ((head - 1 - t) % D + D) % D;
+    S.ctl[0] = cnt; S.ctl[1] = head; S.ctl[2] = push; S.ctl[3] = h;
+    m.best[inst] = best;
+  }
+  sync();
+  const int cnt = S.ctl[0], push = S.ctl[2], h = S.ctl[3];
+  if (push) {
+    for (int j = tid; j < N; j += NT) {
+      hdg[(long long)h * N + j] = graw[j] - gprev[j];
+      hdx[(long long)h * N + j] = w[j + 1] - wprev[j];
+    }
+  }
+  sync();
+  // 3. least squares on the raw mixing residual r: new Gram row <dr_h, dr_s>
+  //    and right-hand side <dr_s, r>, inner products weighted by (f0_j / max f0)^2
+  //    so that nodes whose ||phi - f0|| is far below any tolerance (the walls)
+  //    do not steer the extrapolation
+  if (cnt > 0) {
+    // one history slot at a time: two partial sums live per thread
+    for (int t = 0; t < cnt; t++) {
+      const double *ds_t = hdg + (long long)S.slot[t] * N;
+      double pb = 0.0, pg = 0.0;
+      for (int j = tid; j < N; j += NT) {
+        const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
+        const double gv = graw[j] * wj * wj;
+        const double dh = push ? hdg[(long long)h * N + j] * wj * wj : 0.0;
+        const double d = ds_t[j];
+        pb += d * gv;
+        pg += dh * d;
+      }
+      const double a = warp_sum(pb), b = warp_sum(pg);
+      if (lane == 0) { S.red[t][wid] = a; S.red[MIX_MAXD + t][wid] = b; }
+    }
+    sync();
+    if (tid == 0) {
+      double A[MIX_MAXD * MIX_MAXD], rhs[MIX_MAXD];
+      for (int t = 0; t < cnt; t++) {
+        double sb = 0.0, sg = 0.0;
+        for (int q = 0; q < NW; q++) { sb += S.red[t][q]; sg += S.red[MIX_MAXD + t][q]; }
+        rhs[t] = sb;
+        if (push) { G[h * D + S.slot[t]] = sg; G[S.slot[t] * D + h] = sg; }
+      }
+      double dmax = 0.0;
+      for (int t = 0; t < cnt; t++)
+        for (int u = 0; u < cnt; u++) {
+          A[t * cnt + u] = G[S.slot[t] * D + S.slot[u]];
+          if (t == u) dmax = fmax(dmax, A[t * cnt + u]);
+        }
+      for (int t = 0; t < cnt; t++) A[t * cnt + t] += m.reg * dmax + 1e-300;
+      small_solve(A, rhs, cnt);
+      for (int t = 0; t < cnt; t++) S.gam[t] = rhs[t];
+    }
+    sync();
+  }
+  // 4. mixed residual rbar = r - sum_s gam_s dr_s (into gcur)
+  for (int j = tid; j < N; j += NT) {
+    double rb = graw[j];
+    for (int t = 0; t < cnt; t++) rb -= S.gam[t] * hdg[(long long)S.slot[t] * N + j];
+    gcur[j] = rb;
+  }
+  sync();
+  // 5. update w <- w - sum_s gam_s dx_s + beta (1 + a (-d2/dx2)) rbar
+  //    (the preconditioner acts on the step only, so FP32 rounding noise it
+  //    amplifies never enters the least squares; the mixed residual is
+  //    extended linearly past the first and last interior nodes, i.e. no
+  //    curvature term there); beta = 1 - lk.  The step is scaled so that its
+  //    f0-weighted max norm is <= clip and no node moves by more than
+  //    step_cap / ds; the field is kept >= -field_floor / ds.
+  const double beta = 1.0 - m.lk[inst];
+  const double dsi = m.ds[inst];
+  double dm = 0.0, da = 0.0;
+  for (int j = tid; j < N; j += NT) {
+    const double gc = gcur[j];
+    double lap = 0.0;
+    if (j > 0 && j < N - 1) {
+      const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
+      lap = ((gc - gcur[j - 1]) / a1 + (gc - gcur[j + 1]) / a2) / (0.5 * (a1 + a2));
+    }
+    double d = beta * (gc + m.precond * lap);
+    for (int t = 0; t < cnt; t++) d -= S.gam[t] * hdx[(long long)S.slot[t] * N + j];
+    wprev[j] = d;  // staged; wprev receives the old field below
+    const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
+    dm = fmax(dm, fabs(d) * wj);
+    da = fmax(da, fabs(d));
+  }
+  dm = group_max(dm, S, tid, sync);
+  da = group_max(da, S, tid, sync);
+  double scale = (dm > m.clip) ? m.clip / dm : 1.0;
+  if (m.step_cap > 0.0 && da * scale * dsi > m.step_cap) scale = m.step_cap / (da * dsi);
+  const double wfloor = (m.field_floor > 0.0) ? -m.field_floor / dsi : -INFINITY;
+  for (int j = tid; j < N; j += NT) {
+    const double wo = w[j + 1];
+    const double d = wprev[j];
+    wprev[j] = wo;
+    gprev[j] = graw[j];
+    w[j + 1] = fmax(wo + scale * d, wfloor);
+  }
+  if (tid == 0) {
+    m.iters[inst] = it + 1;
+    m.hcount[inst] = cnt;
+    m.hhead[inst] = S.ctl[1];
+    m.err[inst] = e;
+    if (m.lk_schedule) {
+      double l = m.lk[inst];
+      if (e < 0.03 && it > 100) l *= m.lmd;
+      if (l < 1e-5) l = m.lmd;
+      m.lk[inst] = l;
+    }
+  }
+  sync();
+  return false;
+}
+
+}  // namespace scft

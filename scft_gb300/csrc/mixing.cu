@@ -6,21 +6,12 @@
 //                   preconditioned and clipped step, restart safeguard.
 // admchen_step_*    one iteration of ADM_chen_C.c:55-135 for the drop-in solver.
 // adm_*             one iteration of adm.c:103-306 for the drop-in solver.
-#include "mixing.cuh"
+#include "mix_group.cuh"
 
 namespace scft {
 
 constexpr int MIX_THREADS = 256;
-constexpr int MAXD = 16;
-
-__device__ __forceinline__ double warp_max(double v) {
-  for (int s = 16; s > 0; s >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, s));
-  return v;
-}
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-  return v;
-}
+constexpr int MAXD = MIX_MAXD;
 
 // block-wide max of v (all threads receive it)
 __device__ double block_max(double v, double *sm) {
@@ -34,215 +25,13 @@ __device__ double block_max(double v, double *sm) {
   return r;
 }
 
-// Solve the k x k system A g = b (row-major, A overwritten) by Gaussian
-// elimination with partial pivoting; single thread.
-__device__ void small_solve(double *A, double *b, int k) {
-  for (int c = 0; c < k; c++) {
-    int p = c;
-    double big = fabs(A[c * k + c]);
-    for (int r = c + 1; r < k; r++)
-      if (fabs(A[r * k + c]) > big) { big = fabs(A[r * k + c]); p = r; }
-    if (p != c) {
-      for (int j = 0; j < k; j++) { double t = A[c * k + j]; A[c * k + j] = A[p * k + j]; A[p * k + j] = t; }
-      double t = b[c]; b[c] = b[p]; b[p] = t;
-    }
-    double piv = A[c * k + c];
-    if (piv == 0.0) piv = 1e-300;
-    for (int r = c + 1; r < k; r++) {
-      double f = A[r * k + c] / piv;
-      for (int j = c; j < k; j++) A[r * k + j] -= f * A[c * k + j];
-      b[r] -= f * b[c];
-    }
-  }
-  for (int c = k - 1; c >= 0; c--) {
-    double s = b[c];
-    for (int j = c + 1; j < k; j++) s -= A[c * k + j] * b[j];
-    double piv = A[c * k + c];
-    b[c] = s / (piv == 0.0 ? 1e-300 : piv);
-  }
-}
-
+// One batched Anderson iteration per unfinished instance, one CTA each.
 __global__ void __launch_bounds__(MIX_THREADS) mix_kernel(MixDev m) {
   const int inst = blockIdx.x;
-  const int act = m.active[inst];
-  if (act == 0) return;
-  __shared__ double sm[32];
-  __shared__ double red[2 * MAXD][MIX_THREADS / 32];
-  __shared__ double gam[MAXD];
-  __shared__ int sh_slot[MAXD];
-  __shared__ int sh_ctl[4];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int n = m.n[inst], N = n - 2;
-  const long long no = m.node_off[inst], io = m.int_off[inst];
-  const double *x = m.x + no, *f0 = m.f0 + no, *phi = m.phi + no;
-  double *w = m.w + no;
-  double *graw = m.graw + io, *gcur = m.gcur + io, *gprev = m.gprev + io, *wprev = m.wprev + io;
-  const int D = m.depth;
-  double *hdx = m.hdx + io * D, *hdg = m.hdg + io * D;
-  double *G = m.gram + (long long)inst * D * D;
-
-  // 1. residual, its norm, raw mixing residual
-  double e = 0.0, badv = 0.0;
-  for (int j = tid; j < N; j += MIX_THREADS) {
-    const double p = phi[j + 1], f = f0[j + 1], r = p - f;
-    if (!isfinite(r)) badv = 1.0;
-    e = fmax(e, fabs(r));
-    graw[j] = m.mode ? (log(fmax(p, 1e-300)) - log(f)) : r;
-  }
-  e = block_max(e, sm);
-  badv = block_max(badv, sm);
-  // weights f0_j / max f0: the scale on which ||phi - f0||_inf is judged
-  double fmx = 0.0;
-  if (m.weighted) {
-    for (int j = tid; j < N; j += MIX_THREADS) fmx = fmax(fmx, f0[j + 1]);
-    fmx = block_max(fmx, sm);
-  }
-  const double winv = (m.weighted && fmx > 0.0) ? 1.0 / fmx : 0.0;
-  const int it = m.iters[inst];
-  if (badv != 0.0) {
-    if (tid == 0) { m.status[inst] |= ST_NONFINITE; m.active[inst] = 0; m.err[inst] = e; }
-    return;
-  }
-  const double tol_here = (act == 1) ? m.tol32 : m.tol;
-  if (e <= tol_here) {
-    if (tid == 0) {
-      m.err[inst] = e;
-      if (act == 1 && m.verify64) m.active[inst] = 2;
-      else { m.status[inst] |= ST_CONVERGED; m.active[inst] = 0; }
-    }
-    return;
-  }
-  if (it >= m.maxit) {
-    if (tid == 0) { m.status[inst] |= ST_MAXIT; m.active[inst] = 0; m.err[inst] = e; }
-    return;
-  }
-  // 2. history bookkeeping (restart when the error grew by more than `grow`)
-  if (tid == 0) {
-    int cnt = m.hcount[inst], head = m.hhead[inst];
-    double best = m.best[inst];
-    const bool restart = (it > 0) && (e > m.grow * best);
-    if (restart) { cnt = 0; best = e; m.status[inst] |= ST_RESTARTED; }
-    else best = (it == 0) ? e : fmin(best, e);
-    const int push = (it > 0) && !restart;
-    const int h = head;
-    if (push) { head = (head + 1) % D; cnt = cnt + 1 < D ? cnt + 1 : D; }
-    for (int t = 0; t < cnt; t++) sh_slot[t] = ((head - 1 - t) % D + D) % D;
-    sh_ctl[0] = cnt; sh_ctl[1] = head; sh_ctl[2] = push; sh_ctl[3] = h;
-    m.best[inst] = best;
-  }
-  __syncthreads();
-  const int cnt = sh_ctl[0], push = sh_ctl[2], h = sh_ctl[3];
-  if (push) {
-    for (int j = tid; j < N; j += MIX_THREADS) {
-      hdg[(long long)h * N + j] = graw[j] - gprev[j];
-      hdx[(long long)h * N + j] = w[j + 1] - wprev[j];
-    }
-  }
-  __syncthreads();
-  // 3. least squares on the raw mixing residual r: new Gram row <dr_h, dr_s>
-  //    and right-hand side <dr_s, r>, inner products weighted by (f0_j / max f0)^2
-  //    so that nodes whose ||phi - f0|| is far below any tolerance (the walls)
-  //    do not steer the extrapolation
-  if (cnt > 0) {
-    double pb[MAXD], pg[MAXD];
-#pragma unroll
-    for (int t = 0; t < MAXD; t++) { pb[t] = 0.0; pg[t] = 0.0; }
-    for (int j = tid; j < N; j += MIX_THREADS) {
-      const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
-      const double gv = graw[j] * wj * wj;
-      const double dh = push ? hdg[(long long)h * N + j] * wj * wj : 0.0;
-#pragma unroll
-      for (int t = 0; t < MAXD; t++) {
-        if (t < cnt) {
-          const double d = hdg[(long long)sh_slot[t] * N + j];
-          pb[t] += d * gv;
-          pg[t] += dh * d;
-        }
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < MAXD; t++) {
-      if (t < cnt) {
-        const double a = warp_sum(pb[t]), b = warp_sum(pg[t]);
-        if (lane == 0) { red[t][wid] = a; red[MAXD + t][wid] = b; }
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double A[MAXD * MAXD], rhs[MAXD];
-      for (int t = 0; t < cnt; t++) {
-        double sb = 0.0, sg = 0.0;
-        for (int q = 0; q < MIX_THREADS / 32; q++) { sb += red[t][q]; sg += red[MAXD + t][q]; }
-        rhs[t] = sb;
-        if (push) { G[h * D + sh_slot[t]] = sg; G[sh_slot[t] * D + h] = sg; }
-      }
-      double dmax = 0.0;
-      for (int t = 0; t < cnt; t++)
-        for (int u = 0; u < cnt; u++) {
-          A[t * cnt + u] = G[sh_slot[t] * D + sh_slot[u]];
-          if (t == u) dmax = fmax(dmax, A[t * cnt + u]);
-        }
-      for (int t = 0; t < cnt; t++) A[t * cnt + t] += m.reg * dmax + 1e-300;
-      small_solve(A, rhs, cnt);
-      for (int t = 0; t < cnt; t++) gam[t] = rhs[t];
-    }
-    __syncthreads();
-  }
-  // 4. mixed residual rbar = r - sum_s gam_s dr_s (into gcur)
-  for (int j = tid; j < N; j += MIX_THREADS) {
-    double rb = graw[j];
-    for (int t = 0; t < cnt; t++) rb -= gam[t] * hdg[(long long)sh_slot[t] * N + j];
-    gcur[j] = rb;
-  }
-  __syncthreads();
-  // 5. update w <- w - sum_s gam_s dx_s + beta (1 + a (-d2/dx2)) rbar
-  //    (the preconditioner acts on the step only, so FP32 rounding noise it
-  //    amplifies never enters the least squares; the mixed residual is
-  //    extended linearly past the first and last interior nodes, i.e. no
-  //    curvature term there); beta = 1 - lk.  The step is scaled so that its
-  //    f0-weighted max norm is <= clip and no node moves by more than
-  //    step_cap / ds; the field is kept >= -field_floor / ds.
-  const double beta = 1.0 - m.lk[inst];
-  const double dsi = m.ds[inst];
-  double dm = 0.0, da = 0.0;
-  for (int j = tid; j < N; j += MIX_THREADS) {
-    const double gc = gcur[j];
-    double lap = 0.0;
-    if (j > 0 && j < N - 1) {
-      const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
-      lap = ((gc - gcur[j - 1]) / a1 + (gc - gcur[j + 1]) / a2) / (0.5 * (a1 + a2));
-    }
-    double d = beta * (gc + m.precond * lap);
-    for (int t = 0; t < cnt; t++) d -= gam[t] * hdx[(long long)sh_slot[t] * N + j];
-    wprev[j] = d;  // staged; wprev receives the old field below
-    const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
-    dm = fmax(dm, fabs(d) * wj);
-    da = fmax(da, fabs(d));
-  }
-  dm = block_max(dm, sm);
-  da = block_max(da, sm);
-  double scale = (dm > m.clip) ? m.clip / dm : 1.0;
-  if (m.step_cap > 0.0 && da * scale * dsi > m.step_cap) scale = m.step_cap / (da * dsi);
-  const double wfloor = (m.field_floor > 0.0) ? -m.field_floor / dsi : -INFINITY;
-  for (int j = tid; j < N; j += MIX_THREADS) {
-    const double wo = w[j + 1];
-    const double d = wprev[j];
-    wprev[j] = wo;
-    gprev[j] = graw[j];
-    w[j + 1] = fmax(wo + scale * d, wfloor);
-  }
-  if (tid == 0) {
-    m.iters[inst] = it + 1;
-    m.hcount[inst] = cnt;
-    m.hhead[inst] = sh_ctl[1];
-    m.err[inst] = e;
-    if (m.lk_schedule) {
-      double l = m.lk[inst];
-      if (e < 0.03 && it > 100) l *= m.lmd;
-      if (l < 1e-5) l = m.lmd;
-      m.lk[inst] = l;
-    }
-  }
+  if (m.active[inst] == 0) return;
+  __shared__ MixSmem<MIX_THREADS / 32> S;
+  auto sync = []() { __syncthreads(); };
+  mix_step<MIX_THREADS / 32>(m, inst, threadIdx.x, S, sync);
 }
 
 cudaError_t mix_launch(const MixDev &m, cudaStream_t st) {

@@ -32,6 +32,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "mix_group.cuh"
 
 namespace scft {
 
@@ -122,6 +123,42 @@ struct Propagator {
       instance(b, S, P, lane, wid, inst, slot, bar_id);
       if (cls.work && P == 0)
         atomicAdd(cls.work, (unsigned long long)b.n[inst] * (unsigned long long)(b.nsteps[inst] / 2 + 1));
+    }
+  }
+
+  // Fused solve: the group carries every instance it takes from the queue
+  // through contour pass, Anderson step, contour pass, ... until the mixing
+  // step reports it finished (converged, non-finite or at the iteration
+  // limit), then takes the next one.  No barrier spans more than the group,
+  // so instances with short contours or few iterations never wait for the
+  // slow ones.
+  __device__ static void solve(const BatchDev &b, const ClassDev &cls, const MixDev &m, GroupSmem<R, NW> &S,
+                               MixSmem<NW> &MS, int P, int worker, int bar_id) {
+    const int lane = P & 31, wid = P >> 5;
+    R *slot = reinterpret_cast<R *>(cls.scratch) + (long long)worker * cls.slot_elems;
+    auto sync = [&]() { gsync(bar_id); };
+    for (;;) {
+      int item;
+      if (NW > 1) {
+        if (P == 0) S.item = atomicAdd(cls.head, 1);
+        gsync(bar_id);
+        item = S.item;
+        gsync(bar_id);
+      } else {
+        item = 0;
+        if (lane == 0) item = atomicAdd(cls.head, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+      }
+      if (item >= cls.count) break;
+      const int inst = cls.items[item];
+      if (b.active[inst] != cls.want) continue;
+      for (;;) {
+        instance(b, S, P, lane, wid, inst, slot, bar_id);
+        if (cls.work && P == 0)
+          atomicAdd(cls.work, (unsigned long long)b.n[inst] * (unsigned long long)(b.nsteps[inst] / 2 + 1));
+        gsync(bar_id);  // density, Q and status of this pass visible to the group
+        if (mix_step<NW>(m, inst, P, MS, sync)) break;
+      }
     }
   }
 
@@ -344,7 +381,7 @@ struct Propagator {
         const double a1 = x[i] - x[i - 1], a2 = x[i + 1] - x[i];
         const double ml = a1 / 6.0, md = a1 / 3.0 + a2 / 3.0, mu = a2 / 6.0;
         const double kl = -1.0 / a1, kd = 1.0 / a1 + 1.0 / a2, ku = -1.0 / a2;
-        const double wi = w[i];
+        const double wi = __ldcg(w + i);  // L2: the fused solve updates w between passes
         const double al = kl + wi * ml, ad = kd + wi * md, au = ku + wi * mu;
         dl[c] = (j == 0) ? 0.0 : ml + ds * al;
         dd[c] = md + ds * ad;
@@ -732,6 +769,20 @@ propagate_kernel(BatchDev b, ClassDev cls) {
   const int worker = blockIdx.x * Pp::GPC + g;
   if (worker >= cls.workers) return;
   Pp::run(b, cls, sm[g], P, worker, 1 + g);
+}
+
+// Fused persistent solve of one shape class (see Propagator::solve).
+template <typename R, int C, int NW, bool DELTA>
+__global__ void __launch_bounds__(Propagator<R, C, NW, DELTA>::CTA, 1)
+solve_kernel(BatchDev b, ClassDev cls, MixDev m) {
+  using Pp = Propagator<R, C, NW, DELTA>;
+  __shared__ GroupSmem<R, NW> sm[Pp::GPC];
+  __shared__ MixSmem<NW> ms[Pp::GPC];
+  const int g = threadIdx.x / Pp::T;
+  const int P = threadIdx.x % Pp::T;
+  const int worker = blockIdx.x * Pp::GPC + g;
+  if (worker >= cls.workers) return;
+  Pp::solve(b, cls, m, sm[g], ms[g], P, worker, 1 + g);
 }
 
 }  // namespace scft

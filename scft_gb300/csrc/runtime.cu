@@ -31,6 +31,15 @@ cudaError_t propagate_launch_f32_a(int, int, const BatchDev &, const ClassDev &,
 cudaError_t propagate_launch_f32_b(int, int, const BatchDev &, const ClassDev &, int, cudaStream_t, int *, bool *);
 cudaError_t propagate_launch_f64_a(int, int, const BatchDev &, const ClassDev &, int, cudaStream_t, int *, bool *);
 cudaError_t propagate_launch_f64_b(int, int, const BatchDev &, const ClassDev &, int, cudaStream_t, int *, bool *);
+cudaError_t solve_launch_f32_a(int, int, const BatchDev &, const ClassDev &, const MixDev &, int, cudaStream_t, int *);
+cudaError_t solve_launch_f32_b(int, int, const BatchDev &, const ClassDev &, const MixDev &, int, cudaStream_t, int *);
+
+// Fused FP32 solve of one shape class: launch (ctas == nullptr) or occupancy query.
+static cudaError_t solve_dispatch(int C, int NW, const BatchDev &b, const ClassDev &cls, const MixDev &m, int grid,
+                                  cudaStream_t st, int *ctas) {
+  return NW <= 4 ? solve_launch_f32_a(C, NW, b, cls, m, grid, st, ctas)
+                 : solve_launch_f32_b(C, NW, b, cls, m, grid, st, ctas);
+}
 
 static cudaError_t dispatch(int prec, int C, int NW, const BatchDev &b, const ClassDev &cls, int grid,
                             cudaStream_t st, int *ctas, bool *exists) {
@@ -588,19 +597,11 @@ static int evaluate(scft_batch *B, int p) {
   return SCFT_OK;
 }
 
-static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
-  const int p = o->precision;
-  if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
-      !(o->beta > 0.0 && o->beta <= 1.0))
-    return set_err(SCFT_EINVAL, "solve options");
-  int rc = plan(B, p, 1.0);
-  if (rc) return rc;
-  const bool verify = (p == PREC_F32) && o->verify64;
-  if (verify && (rc = plan(B, PREC_F64, 0.125))) return rc;
-  if ((rc = ensure_mix(B, o->depth))) return rc;
+// Reset the per-instance solver state on B->st and describe it to the mixing step.
+static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool verify, MixDev *mp) {
   cudaStream_t st = B->st;
   const int c = B->count;
-  CK(cudaEventRecord(B->t0, st));
+  int rc;
   if ((rc = fill_int(B->d_active, c, p == PREC_F32 ? 1 : 2, st))) return rc;
   CK(cudaMemsetAsync(B->d_status, 0, c * sizeof(int), st));
   CK(cudaMemsetAsync(B->d_iters, 0, c * sizeof(int), st));
@@ -611,7 +612,7 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   if ((rc = fill_double(B->d_lk, c, 1.0 - o->beta, st))) return rc;
   if ((rc = fill_double(B->d_err, c, INFINITY, st))) return rc;
 
-  MixDev m;
+  MixDev &m = *mp;
   m.count = c;
   m.n = B->d_n;
   m.node_off = B->d_node_off;
@@ -626,6 +627,92 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   m.tol = o->tol; m.tol32 = o->tol * o->tol32_factor; m.clip = o->clip;
   m.grow = o->grow; m.precond = o->precond; m.reg = o->reg;
   m.ds = B->d_ds; m.weighted = o->weighted; m.step_cap = o->step_cap; m.field_floor = o->field_floor;
+  return SCFT_OK;
+}
+
+// Copy the per-instance outcome of the last solve to the caller.
+static int solve_results(scft_batch *B, scft_result *res) {
+  if (!res) return SCFT_OK;
+  const int c = B->count;
+  std::vector<int> stt(c), its(c);
+  std::vector<double> err(c), Q(c);
+  CK(cudaMemcpy(stt.data(), B->d_status, c * sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(its.data(), B->d_iters, c * sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(err.data(), B->d_err, c * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(Q.data(), B->d_Q, c * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < c; i++) { res[i].status = stt[i]; res[i].iterations = its[i]; res[i].err = err[i]; res[i].Q = Q[i]; }
+  return SCFT_OK;
+}
+
+// Fused FP32 solve: one persistent launch per shape class, all classes on
+// forked streams.  Each thread group takes instances from its class queue
+// (most expensive first) and iterates each one to the end on its own, the
+// contour pass and the Anderson step back to back, so no instance waits for a
+// batch-wide iteration.  Every loop is bounded by the iteration limit.
+static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+  const int p = PREC_F32;
+  int rc;
+  if ((rc = live_prepare(B, 1))) return rc;
+  cudaStream_t st = B->st;
+  auto &plans = B->plans[p];
+  CK(cudaEventRecord(B->t0, st));
+  MixDev m;
+  if ((rc = solve_begin(B, o, p, false, &m))) return rc;
+  const size_t live_bytes = (size_t)2 * B->live_maxc * sizeof(unsigned long long);
+  CK(cudaMemsetAsync(B->d_work, 0, live_bytes, st));
+  for (auto &c : plans) CK(cudaMemsetAsync(B->d_heads + c.head, 0, sizeof(int), st));
+  const BatchDev b = batch_dev(B);
+  const auto t_start = std::chrono::steady_clock::now();
+  CK(cudaEventRecord(B->ev_fork, st));
+  for (size_t i = 0; i < plans.size(); i++) {
+    const ClassPlan &c = plans[i];
+    cudaStream_t s = B->side[i];
+    CK(cudaStreamWaitEvent(s, B->ev_fork, 0));
+    ClassDev d;
+    class_dev(B, c, &d);
+    const int li = live_index(B, 0, p, (int)i);
+    d.work = B->d_work + li;
+    // keep the class's share resident if the fused kernel fits fewer CTAs per SM
+    int grid = c.grid, occ = 0;
+    CK(solve_dispatch(c.C, c.NW, b, d, m, 0, s, &occ));
+    const int pocc = propagate_ctas_per_sm(p, c.C, c.NW);
+    if (occ <= 0) return set_err(SCFT_ECUDA, "fused solve of class (%d, %d) does not fit an SM", c.C, c.NW);
+    if (pocc > occ) grid = std::max(1, (int)((long long)c.grid * occ / pocc));
+    d.workers = std::min(c.workers, grid * c.gpc);
+    CK(cudaEventRecord(B->ev_live[2 * li], s));
+    CK(solve_dispatch(c.C, c.NW, b, d, m, grid, s, nullptr));
+    g_launches++;
+    CK(cudaEventRecord(B->ev_live[2 * li + 1], s));
+    CK(cudaEventRecord(B->ev_join[i], s));
+  }
+  for (size_t i = 0; i < plans.size(); i++) CK(cudaStreamWaitEvent(st, B->ev_join[i], 0));
+  CK(cudaMemcpyAsync(B->h_work, B->d_work, live_bytes, cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(B->t1, st));
+  cudaError_t e = cudaEventSynchronize(B->t1);
+  if (e != cudaSuccess) return set_err(SCFT_ECUDA, "fused solve: %s", cudaGetErrorString(e));
+  if ((rc = live_collect(B, 1, true, false))) return rc;
+  B->trace_active.assign(1, 0);
+  B->trace_ms.assign(1, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
+  CK(cudaEventElapsedTime(&B->last_ms, B->t0, B->t1));
+  return solve_results(B, res);
+}
+
+static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+  const int p = o->precision;
+  if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
+      !(o->beta > 0.0 && o->beta <= 1.0))
+    return set_err(SCFT_EINVAL, "solve options");
+  int rc = plan(B, p, 1.0);
+  if (rc) return rc;
+  const bool verify = (p == PREC_F32) && o->verify64;
+  if ((rc = ensure_mix(B, o->depth))) return rc;
+  if (o->fused && p == PREC_F32 && !verify) return solve_fused(B, o, res);
+  if (verify && (rc = plan(B, PREC_F64, 0.125))) return rc;
+  cudaStream_t st = B->st;
+  const int c = B->count;
+  CK(cudaEventRecord(B->t0, st));
+  MixDev m;
+  if ((rc = solve_begin(B, o, p, verify, &m))) return rc;
 
   const int K = std::max(1, o->iters_per_graph);
   // capture K iterations: propagate (FP32 and/or FP64 classes), mix; then count
@@ -692,16 +779,7 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   CK(cudaEventRecord(B->t1, st));
   CK(cudaEventSynchronize(B->t1));
   CK(cudaEventElapsedTime(&B->last_ms, B->t0, B->t1));
-  if (res) {
-    std::vector<int> stt(c), its(c);
-    std::vector<double> err(c), Q(c);
-    CK(cudaMemcpy(stt.data(), B->d_status, c * sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(its.data(), B->d_iters, c * sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(err.data(), B->d_err, c * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(Q.data(), B->d_Q, c * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int i = 0; i < c; i++) { res[i].status = stt[i]; res[i].iterations = its[i]; res[i].err = err[i]; res[i].Q = Q[i]; }
-  }
-  return SCFT_OK;
+  return solve_results(B, res);
 }
 
 // ---------------------------------------------------------------------------
@@ -1335,17 +1413,18 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->verify64 = 0;
   o->maxit = 2000;
   o->depth = 10;
-  o->beta = 0.1;
+  o->beta = 1.0;
   o->clip = 1.0;
   o->grow = 10.0;
   o->reg = 1e-12;
   o->residual_mode = SCFT_MIX_LOG;
-  o->precond = 1.0 / 6.0;
+  o->precond = 0.6;
   o->iters_per_graph = 8;
-  o->beta_schedule = 1;
+  o->beta_schedule = 0;
   o->weighted = 1;
   o->step_cap = 0.25;
   o->field_floor = 0.5;
+  o->fused = 1;
 }
 
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {

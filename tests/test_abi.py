@@ -55,7 +55,7 @@ def test_strerror_and_defaults_without_device():
     assert lib.scft_strerror(_lib.SCFT_ENODEV) == b"no CUDA device"
     from scft_gb300 import api
     o = api.solve_opts()
-    assert o.depth == 10 and o.beta == pytest.approx(0.1) and o.precision == _lib.F32
+    assert o.depth == 10 and o.beta == pytest.approx(1.0) and o.fused == 1 and o.precision == _lib.F32
     import ctypes as C
     c = _lib.ScftConfig()
     lib.scft_config_init(C.byref(c))
