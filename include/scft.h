@@ -23,6 +23,7 @@ extern "C" {
 #define SCFT_ENOCONFIG (-4) /* scft_set_config was not called */
 #define SCFT_ENODEV (-5)    /* no CUDA device */
 #define SCFT_ESINGULAR (-6) /* singular Jacobian (Broyden) */
+#define SCFT_EIO (-7)       /* a file could not be opened, read or written */
 
 /* ---- per-instance result status bits ---- */
 #define SCFT_ST_NOT_DOMINANT 1 /* 1 + ds*w < 0 somewhere: system lost diagonal dominance */
@@ -281,6 +282,33 @@ const char *scft_ws_last_error(void);
  * ========================================================================= */
 int scft_density_noalloc(int n_nodes, const double *x, const double *w, int nsteps, double ds, int rule,
                          int precision, double *phi, double *Q, void *stream);
+
+/* =========================================================================
+ * The reference's field files (host only; no device is needed).
+ * ========================================================================= */
+
+/* Reads a field file in the form DEALII_SCFT/src/scft.cc:317-333 writes and
+   DEALII_SCFT/src/scft_util.cc:14-41 (read_yita_middle_1D) reads:
+     "N= <nodes>, ERROR= <e>", "mean_field_free_energy, <F>", then "i,x_i,w_i"
+   per node.  The MATLAB inputs (Matlab_files/inputFiles/solution_yita_1D_N=*.txt,
+   first line "N= <nodes>" only, no energy line) are read too.  *n_nodes receives
+   N (also when N > max_nodes, which returns SCFT_EINVAL); x and w (max_nodes
+   doubles, either may be NULL) receive the nodes; *err and *free_energy (may be
+   NULL) receive the header values or NAN when the file has none.  Every node
+   0..N-1 must be present.  SCFT_EIO when the file cannot be opened. */
+int scft_field_read(const char *path, int max_nodes, int *n_nodes, double *x, double *w, double *err,
+                    double *free_energy);
+/* Writes the form above with the reference's formats ("%e" error, "%2.15f"
+   energy and values), so read_yita_middle_1D reads it back. */
+int scft_field_write(const char *path, int n_nodes, const double *x, const double *w, double err,
+                     double free_energy);
+/* Reads a .res table of the external implicit-Euler code (the file
+   1D_FEM.c:321-342 takes its starting field from): every row of five numbers
+   (x/l, phi, eta, phie, phij; walls included) into table (row-major, max_rows x
+   5), *rows = rows found (SCFT_EINVAL when above max_rows), *m and *nsteps from
+   "m = <m>   n = <steps>" (-1 when absent), header[6] = l, mphi, t, Z, f,
+   |f|max (NAN when absent; may be NULL). */
+int scft_res_read(const char *path, int max_rows, int *rows, double *table, int *m, int *nsteps, double *header);
 
 /* Kernels launched by this library since load (graph replays count each node). */
 long long scft_kernel_launches(void);

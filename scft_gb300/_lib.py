@@ -18,6 +18,7 @@ SCFT_ENOMEM = -3
 SCFT_ENOCONFIG = -4
 SCFT_ENODEV = -5
 SCFT_ESINGULAR = -6
+SCFT_EIO = -7
 
 ST_NOT_DOMINANT = 1
 ST_NONFINITE = 2
@@ -110,6 +111,10 @@ SIGNATURES = {
     "scft_ws_last_error": (C.c_char_p, []),
     "scft_density_noalloc": (C.c_int, [C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp,
                                        C.c_void_p]),
+    "scft_field_read": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), _dp, _dp, _dp, _dp]),
+    "scft_field_write": (C.c_int, [C.c_char_p, C.c_int, _dp, _dp, C.c_double, C.c_double]),
+    "scft_res_read": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), _dp, C.POINTER(C.c_int),
+                                C.POINTER(C.c_int), _dp]),
 }
 
 _lib = None

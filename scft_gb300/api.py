@@ -112,6 +112,51 @@ def density(w_nodes: np.ndarray):
 
 
 # ---------------------------------------------------------------------------
+# the reference's field files
+# ---------------------------------------------------------------------------
+def read_field(path: str, max_nodes: int = 1 << 20):
+    """Field file of scft.cc:317-333 / read_yita_middle_1D (scft_util.cc:14-41),
+    MATLAB inputs included.  Returns dict(x, w, err, free_energy); absent header
+    values are NaN."""
+    lib = L.load()
+    n = C.c_int()
+    err, F = C.c_double(), C.c_double()
+    rc = lib.scft_field_read(path.encode(), 0, C.byref(n), None, None, None, None)
+    if rc != 0 and n.value <= 0:
+        check(rc, "scft_field_read")
+    x = np.empty(n.value)
+    w = np.empty(n.value)
+    check(lib.scft_field_read(path.encode(), min(n.value, max_nodes), C.byref(n), _dp(x), _dp(w), C.byref(err),
+                              C.byref(F)), "scft_field_read")
+    return {"x": x, "w": w, "err": err.value, "free_energy": F.value}
+
+
+def write_field(path: str, x, w, err: float, free_energy: float):
+    """Write a field file read_yita_middle_1D reads back (scft.cc:317-333 formats)."""
+    xa = np.ascontiguousarray(x, dtype=np.float64)
+    wa = np.ascontiguousarray(w, dtype=np.float64)
+    if xa.shape != wa.shape:
+        raise ValueError("x and w differ in length")
+    check(L.load().scft_field_write(path.encode(), len(xa), _dp(xa), _dp(wa), float(err), float(free_energy)),
+          "scft_field_write")
+
+
+def read_res(path: str, max_rows: int = 1 << 20):
+    """.res table (the starting field of 1D_FEM.c:321-342): columns x/l, phi, eta,
+    phie, phij for every node, and the header values."""
+    lib = L.load()
+    rows, m, ns = C.c_int(), C.c_int(), C.c_int()
+    hdr = np.empty(6)
+    table = np.empty((max_rows, 5))
+    check(lib.scft_res_read(path.encode(), max_rows, C.byref(rows), _dp(table), C.byref(m), C.byref(ns), _dp(hdr)),
+          "scft_res_read")
+    t = table[:rows.value]
+    out = {k: t[:, i].copy() for i, k in enumerate(("x_over_l", "phi", "eta", "phie", "phij"))}
+    out.update(m=m.value, nsteps=ns.value, **dict(zip(("l", "mphi", "t", "Z", "f", "fmax"), hdr)))
+    return out
+
+
+# ---------------------------------------------------------------------------
 # solvers
 # ---------------------------------------------------------------------------
 def adm(x, n, f, flag=0, maxit=1000000):

@@ -1192,6 +1192,7 @@ const char *scft_strerror(int code) {
     case SCFT_ENOCONFIG: return "scft_set_config was not called";
     case SCFT_ENODEV: return "no CUDA device";
     case SCFT_ESINGULAR: return "singular Jacobian";
+    case SCFT_EIO: return "file error";
     default: return "unknown error";
   }
 }
