@@ -32,6 +32,7 @@ extern "C" {
 #define SCFT_ST_MAXIT 8
 #define SCFT_ST_RESTARTED 16   /* the Anderson history was restarted at least once */
 #define SCFT_ST_WATCHDOG 32    /* the host loop stopped on its launch cap */
+#define SCFT_ST_FP64 64        /* the FP32 iteration stalled and the FP64 propagator finished the solve */
 
 enum { SCFT_RULE_ROMBERG = 0, SCFT_RULE_TRAPEZOID = 1 };
 enum { SCFT_F32 = 0, SCFT_F64 = 1 };
@@ -152,6 +153,11 @@ typedef struct scft_solve_opts {
                          class (contour pass and Anderson step by the same thread group, no barrier
                          across the batch; FP32 without verify64); 0: every iteration is a batch-wide
                          step (propagator launches, then the mixing kernel) replayed from CUDA graphs */
+  int finish_stall;   /* FP32 solves: an instance whose error is below finish_tol and has not halved
+                         for this many iterations continues with the FP64 propagator (fresh Anderson
+                         history, tolerance tol, status bit SCFT_ST_FP64); 0: off.  FP32 rounding
+                         noise in the density (~1e-7) corrupts the secant pairs of small steps */
+  double finish_tol;
 } scft_solve_opts;
 
 typedef struct scft_result {

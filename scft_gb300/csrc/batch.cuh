@@ -38,7 +38,8 @@ struct scft_batch {
   int depth = 0;
   double *d_graw = nullptr, *d_gcur = nullptr, *d_gprev = nullptr, *d_wprev = nullptr;
   double *d_hdx = nullptr, *d_hdg = nullptr, *d_gram = nullptr, *d_err = nullptr, *d_best = nullptr;
-  double *d_lk = nullptr;
+  double *d_lk = nullptr, *d_ref_err = nullptr;
+  int *d_ref_it = nullptr;
   int *d_iters = nullptr, *d_hcount = nullptr, *d_hhead = nullptr, *d_nactive = nullptr;
   int *h_nactive = nullptr;
   std::vector<int> trace_active;   // unfinished instances after each graph launch of the last solve

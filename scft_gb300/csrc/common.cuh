@@ -43,6 +43,7 @@ enum : int {
   ST_MAXIT = 8,
   ST_RESTARTED = 16,
   ST_WATCHDOG = 32,
+  ST_FP64 = 64,
 };
 
 }  // namespace scft

@@ -130,14 +130,33 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     if (tid == 0) { m.status[inst] |= ST_MAXIT; m.active[inst] = 0; m.err[inst] = e; }
     return true;
   }
+  // FP32 stall: below finish_tol and no halving of the error for finish_stall
+  // iterations -> the FP64 propagator continues from this field with a fresh
+  // history (the FP32 density's rounding noise, ~1e-7, spoils the secant pairs
+  // of the small steps near convergence)
+  const int rit = m.ref_it[inst];
+  if (act == 1 && m.finish_stall > 0 && e < m.finish_tol && rit >= 0 && it - rit >= m.finish_stall) {
+    if (tid == 0) {
+      m.active[inst] = 2;
+      m.status[inst] |= ST_FP64;
+      m.err[inst] = e;
+      m.hcount[inst] = 0;
+      m.best[inst] = INFINITY;
+      m.ref_err[inst] = INFINITY;
+      m.ref_it[inst] = -1;
+    }
+    return true;
+  }
   // 2. history bookkeeping (restart when the error grew by more than `grow`)
   if (tid == 0) {
     int cnt = m.hcount[inst], head = m.hhead[inst];
     double best = m.best[inst];
-    const bool restart = (it > 0) && (e > m.grow * best);
+    const bool fresh = (it == 0) || (rit < 0);
+    const bool restart = !fresh && (e > m.grow * best);
     if (restart) { cnt = 0; best = e; m.status[inst] |= ST_RESTARTED; }
-    else best = (it == 0) ? e : fmin(best, e);
-    const int push = (it > 0) && !restart;
+    else best = fresh ? e : fmin(best, e);
+    if (fresh || e < 0.5 * m.ref_err[inst]) { m.ref_err[inst] = e; m.ref_it[inst] = it; }
+    const int push = !fresh && !restart;
     const int h = head;
     if (push) { head = (head + 1) % D; cnt = cnt + 1 < D ? cnt + 1 : D; }
     for (int t = 0; t < cnt; t++) S.slot[t] = ((head - 1 - t) % D + D) % D;

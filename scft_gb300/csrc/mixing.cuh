@@ -34,6 +34,13 @@ struct MixDev {
   int weighted;       // least squares and clip weighted by f0 / max f0
   double step_cap;    // |step_i| <= step_cap / ds (0: off)
   double field_floor; // w_i >= -field_floor / ds (0: off)
+  // FP32 stall hand-off: ref_err / ref_it = error and iteration of the last
+  // halving of the error; ref_it < 0 marks a history that starts afresh (the
+  // first evaluation after a hand-off pushes no difference pair)
+  int finish_stall;   // 0: off
+  double finish_tol;
+  double *ref_err;
+  int *ref_it;
 };
 
 cudaError_t mix_launch(const MixDev &m, cudaStream_t st);

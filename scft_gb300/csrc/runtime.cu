@@ -447,6 +447,7 @@ static int fill_double(double *a, long long n, double v, cudaStream_t st) {
 static void free_mix(scft_batch *B) {
   dfree(B->d_graw); dfree(B->d_gcur); dfree(B->d_gprev); dfree(B->d_wprev);
   dfree(B->d_hdx); dfree(B->d_hdg); dfree(B->d_gram); dfree(B->d_err); dfree(B->d_best); dfree(B->d_lk);
+  dfree(B->d_ref_err); dfree(B->d_ref_it);
   dfree(B->d_iters); dfree(B->d_hcount); dfree(B->d_hhead); dfree(B->d_nactive);
   if (B->h_nactive) cudaFreeHost(B->h_nactive);
   B->h_nactive = nullptr;
@@ -462,7 +463,8 @@ static int ensure_mix(scft_batch *B, int depth) {
       (rc = dalloc(&B->d_wprev, ni)) || (rc = dalloc(&B->d_hdx, ni * depth)) ||
       (rc = dalloc(&B->d_hdg, ni * depth)) || (rc = dalloc(&B->d_gram, c * depth * depth)) ||
       (rc = dalloc(&B->d_err, c)) || (rc = dalloc(&B->d_best, c)) || (rc = dalloc(&B->d_lk, c)) || (rc = dalloc(&B->d_iters, c)) ||
-      (rc = dalloc(&B->d_hcount, c)) || (rc = dalloc(&B->d_hhead, c)) || (rc = dalloc(&B->d_nactive, 1)))
+      (rc = dalloc(&B->d_hcount, c)) || (rc = dalloc(&B->d_hhead, c)) || (rc = dalloc(&B->d_nactive, 1)) ||
+      (rc = dalloc(&B->d_ref_err, c)) || (rc = dalloc(&B->d_ref_it, c)))
     return rc;
   CK(cudaMallocHost(&B->h_nactive, sizeof(int)));
   B->depth = depth;
@@ -611,6 +613,8 @@ static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool veri
   if ((rc = fill_double(B->d_best, c, INFINITY, st))) return rc;
   if ((rc = fill_double(B->d_lk, c, 1.0 - o->beta, st))) return rc;
   if ((rc = fill_double(B->d_err, c, INFINITY, st))) return rc;
+  if ((rc = fill_double(B->d_ref_err, c, INFINITY, st))) return rc;
+  CK(cudaMemsetAsync(B->d_ref_it, 0, c * sizeof(int), st));
 
   MixDev &m = *mp;
   m.count = c;
@@ -627,6 +631,9 @@ static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool veri
   m.tol = o->tol; m.tol32 = o->tol * o->tol32_factor; m.clip = o->clip;
   m.grow = o->grow; m.precond = o->precond; m.reg = o->reg;
   m.ds = B->d_ds; m.weighted = o->weighted; m.step_cap = o->step_cap; m.field_floor = o->field_floor;
+  m.finish_stall = (p == PREC_F32) ? o->finish_stall : 0;
+  m.finish_tol = o->finish_tol;
+  m.ref_err = B->d_ref_err; m.ref_it = B->d_ref_it;
   return SCFT_OK;
 }
 
@@ -643,6 +650,8 @@ static int solve_results(scft_batch *B, scft_result *res) {
   for (int i = 0; i < c; i++) { res[i].status = stt[i]; res[i].iterations = its[i]; res[i].err = err[i]; res[i].Q = Q[i]; }
   return SCFT_OK;
 }
+
+static int graph_iterate(scft_batch *B, const scft_solve_opts *o, const MixDev &m, bool f32, bool f64);
 
 // Fused FP32 solve: one persistent launch per shape class, all classes on
 // forked streams.  Each thread group takes instances from its class queue
@@ -691,31 +700,38 @@ static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res
   cudaError_t e = cudaEventSynchronize(B->t1);
   if (e != cudaSuccess) return set_err(SCFT_ECUDA, "fused solve: %s", cudaGetErrorString(e));
   if ((rc = live_collect(B, 1, true, false))) return rc;
-  B->trace_active.assign(1, 0);
+  // instances whose FP32 iteration stalled (active == 2) finish with the FP64
+  // propagator, batch-wide iterations over those instances only
+  count_active_kernel<<<1, 256, 0, st>>>(B->d_active, B->count, B->d_nactive);
+  g_launches++;
+  CK(cudaMemcpyAsync(B->h_nactive, B->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  B->trace_active.assign(1, *B->h_nactive);
   B->trace_ms.assign(1, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
+  if (*B->h_nactive > 0) {
+    if ((rc = plan(B, PREC_F64, 1.0))) return rc;
+    std::vector<double> ms32 = B->live_ms[PREC_F32], un32 = B->live_units[PREC_F32];
+    std::vector<long long> ln32 = B->live_launches[PREC_F32];
+    if ((rc = graph_iterate(B, o, m, false, true))) return rc;
+    // keep the fused launch's statistics for the FP32 classes
+    B->live_ms[PREC_F32] = ms32; B->live_units[PREC_F32] = un32; B->live_launches[PREC_F32] = ln32;
+    CK(cudaEventRecord(B->t1, st));
+    CK(cudaEventSynchronize(B->t1));
+  }
   CK(cudaEventElapsedTime(&B->last_ms, B->t0, B->t1));
   return solve_results(B, res);
 }
 
-static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
-  const int p = o->precision;
-  if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
-      !(o->beta > 0.0 && o->beta <= 1.0))
-    return set_err(SCFT_EINVAL, "solve options");
-  int rc = plan(B, p, 1.0);
-  if (rc) return rc;
-  const bool verify = (p == PREC_F32) && o->verify64;
-  if ((rc = ensure_mix(B, o->depth))) return rc;
-  if (o->fused && p == PREC_F32 && !verify) return solve_fused(B, o, res);
-  if (verify && (rc = plan(B, PREC_F64, 0.125))) return rc;
+// Batch-wide iterations replayed from a CUDA graph until no instance is active:
+// each captured iteration launches the propagator classes of the requested
+// precisions (each class evaluates the instances whose active flag it serves),
+// then the mixing kernel; K iterations per graph, then the host reads the count
+// of unfinished instances.
+static int graph_iterate(scft_batch *B, const scft_solve_opts *o, const MixDev &m, bool f32, bool f64) {
   cudaStream_t st = B->st;
   const int c = B->count;
-  CK(cudaEventRecord(B->t0, st));
-  MixDev m;
-  if ((rc = solve_begin(B, o, p, verify, &m))) return rc;
-
+  int rc;
   const int K = std::max(1, o->iters_per_graph);
-  // capture K iterations: propagate (FP32 and/or FP64 classes), mix; then count
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   long long per_graph = 0;
@@ -726,8 +742,8 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   int crc = SCFT_OK;
   if (cudaMemsetAsync(B->d_work, 0, live_bytes, st) != cudaSuccess) crc = set_err(SCFT_ECUDA, "live reset");
   for (int k = 0; k < K && !crc; k++) {
-    if (p == PREC_F32) crc = enqueue_propagate(B, PREC_F32, k);
-    if (!crc && (p == PREC_F64 || verify)) crc = enqueue_propagate(B, PREC_F64, k);
+    if (f32) crc = enqueue_propagate(B, PREC_F32, k);
+    if (!crc && f64) crc = enqueue_propagate(B, PREC_F64, k);
     if (!crc) {
       cudaError_t e = mix_launch(m, st);
       g_launches++;
@@ -750,17 +766,16 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   CK(ec);
   const long long max_launch = (long long)o->maxit / K + 3;
   int result = SCFT_OK;
-  B->trace_active.clear();
-  B->trace_ms.clear();
   const auto t_start = std::chrono::steady_clock::now();
+  const double t_base = B->trace_ms.empty() ? 0.0 : B->trace_ms.back();
   for (long long L = 0;; L++) {
     cudaError_t e = cudaGraphLaunch(gexec, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { result = set_err(SCFT_ECUDA, "solver graph: %s", cudaGetErrorString(e)); break; }
     g_launches += per_graph;
-    if ((rc = live_collect(B, K, p == PREC_F32, p == PREC_F64 || verify))) { result = rc; break; }
+    if ((rc = live_collect(B, K, f32, f64))) { result = rc; break; }
     B->trace_active.push_back(*B->h_nactive);
-    B->trace_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
+    B->trace_ms.push_back(t_base + std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
     if (*B->h_nactive == 0) break;
     if (L + 1 >= max_launch) {
       // watchdog: the mixing kernel stops every instance at maxit, so this is a backstop
@@ -775,7 +790,28 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
     }
   }
   cudaGraphExecDestroy(gexec);
-  if (result) return result;
+  return result;
+}
+
+static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+  const int p = o->precision;
+  if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
+      !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0)
+    return set_err(SCFT_EINVAL, "solve options");
+  int rc = plan(B, p, 1.0);
+  if (rc) return rc;
+  const bool verify = (p == PREC_F32) && o->verify64;
+  const bool need64 = (p == PREC_F64) || verify || o->finish_stall > 0;
+  if ((rc = ensure_mix(B, o->depth))) return rc;
+  if (o->fused && p == PREC_F32 && !verify) return solve_fused(B, o, res);
+  if (p == PREC_F32 && need64 && (rc = plan(B, PREC_F64, 0.125))) return rc;
+  cudaStream_t st = B->st;
+  CK(cudaEventRecord(B->t0, st));
+  MixDev m;
+  if ((rc = solve_begin(B, o, p, verify, &m))) return rc;
+  B->trace_active.clear();
+  B->trace_ms.clear();
+  if ((rc = graph_iterate(B, o, m, p == PREC_F32, need64))) return rc;
   CK(cudaEventRecord(B->t1, st));
   CK(cudaEventSynchronize(B->t1));
   CK(cudaEventElapsedTime(&B->last_ms, B->t0, B->t1));
@@ -1426,6 +1462,8 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->step_cap = 0.25;
   o->field_floor = 0.5;
   o->fused = 1;
+  o->finish_stall = 0;
+  o->finish_tol = 1e-4;
 }
 
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {
