@@ -8,8 +8,9 @@ the batched FP32 propagator and FP64 Anderson mixing (learned warm start when a
 trained network is available), starting from fields resident in HBM.  `value`
 is converged solves per second of the whole job, device-timed with CUDA events
 on the library's stream; `e2e` repeats the measurement through the public C ABI
-with host buffers (batch creation with its host-to-device copies, solve, and the
-device-to-host read of fields and densities inside the timed region).
+with host buffers (batch creation from the caller's concatenated host arrays
+with its host-to-device copies, solve, and the device-to-host read of fields and
+densities inside the timed region).
 
 Under torchrun (N > 1) every rank solves its cost-balanced share of the batch;
 there is no data-path collective ("weak" scaling with the batch split).
@@ -398,23 +399,30 @@ def ours_arm(args):
     # end to end through the C ABI with host buffers
     if not args.no_e2e:
         h2d, d2h = instance_bytes(mine)
-        e2e_s, e2e_conv = [], []
+        host = api.Batch.pack(mine)  # the caller's host buffers: node arrays concatenated, as the C ABI takes them
+        e2e_s, e2e_conv, parts = [], [], []
         for k in range(args.steps + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            with api.Batch(mine) as b2:
+            with api.Batch.from_arrays(host) as b2:
+                t1 = time.perf_counter()
                 if ws is not None:
                     ws.predict(b2)
                 r = b2.solve(opts)
+                t2 = time.perf_counter()
                 b2.get()
+                t3 = time.perf_counter()
             torch.cuda.synchronize()
             if k > 0:
                 e2e_s.append(time.perf_counter() - t0)
                 e2e_conv.append(int(((r["status"] & ST_CONVERGED) != 0).sum()))
+                parts.append((t1 - t0, t2 - t1, t3 - t2))
         es = allreduce_max(torch, world, statistics.mean(e2e_s))
         ec = allreduce_sum(torch, world, statistics.mean(e2e_conv))
         line["e2e"] = {"value": ec / es, "unit": UNIT, "h2d_bytes_per_step": h2d * world,
-                       "d2h_bytes_per_step": d2h * world}
+                       "d2h_bytes_per_step": d2h * world,
+                       "host_ms": {k: 1e3 * statistics.mean(p[i] for p in parts)
+                                   for i, k in enumerate(("create_and_upload", "warm_start_and_solve", "download"))}}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = cpu_sample(mine, args.cpu_sample)

@@ -316,6 +316,13 @@ int scft_field_write(const char *path, int n_nodes, const double *x, const doubl
    |f|max (NAN when absent; may be NULL). */
 int scft_res_read(const char *path, int max_rows, int *rows, double *table, int *m, int *nsteps, double *header);
 
+/* The library keeps the device and pinned host blocks it releases (batches,
+   scratch, warm-start buffers) for reuse, so creating a batch per request does
+   not call cudaMalloc/cudaFree again; a failed allocation releases the cache and
+   retries.  This returns the cached blocks of the current device and the cached
+   pinned blocks to CUDA and reports the bytes released. */
+long long scft_mem_trim(void);
+
 /* Kernels launched by this library since load (graph replays count each node). */
 long long scft_kernel_launches(void);
 

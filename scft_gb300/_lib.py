@@ -98,6 +98,7 @@ SIGNATURES = {
     "scft_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "scft_batch_destroy": (C.c_int, [C.c_void_p]),
     "scft_kernel_launches": (C.c_longlong, []),
+    "scft_mem_trim": (C.c_longlong, []),
     "scft_ws_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "scft_ws_destroy": (C.c_int, [C.c_void_p]),
     "scft_ws_param_count": (C.c_int, [C.c_void_p]),

@@ -213,32 +213,76 @@ class Batch:
     ``instances`` is a sequence of dicts with keys n_nodes, L, f0, nsteps, ds and
     optional x, w0, rule."""
 
-    def __init__(self, instances):
+    def __init__(self, instances=None, *, arrays=None):
+        """From a sequence of instance dicts, or from `arrays` (the output of
+        Batch.pack: node arrays already concatenated)."""
         self.lib = L.load()
-        self.count = len(instances)
-        self._keep = []
-        arr = (L.ScftInstance * self.count)()
-        self.n_nodes = np.empty(self.count, dtype=np.int64)
-        for i, d in enumerate(instances):
-            f0 = np.ascontiguousarray(d["f0"], dtype=np.float64)
-            x = None if d.get("x") is None else np.ascontiguousarray(d["x"], dtype=np.float64)
-            w0 = None if d.get("w0") is None else np.ascontiguousarray(d["w0"], dtype=np.float64)
-            self._keep += [f0, x, w0]
-            s = arr[i]
-            s.n_nodes = int(d["n_nodes"])
-            s.x = _dp(x)
-            s.L = float(d.get("L", 0.0))
-            s.f0 = _dp(f0)
-            s.w0 = _dp(w0)
-            s.nsteps = int(d["nsteps"])
-            s.ds = float(d["ds"])
-            s.rule = int(d.get("rule", L.RULE_ROMBERG))
-            self.n_nodes[i] = s.n_nodes
+        a = arrays if arrays is not None else Batch.pack(instances)
+        self.count = len(a["n_nodes"])
+        self.n_nodes = a["n_nodes"]
         self.offsets = np.concatenate([[0], np.cumsum(self.n_nodes)])
+        desc = Batch._descriptors(a, self.offsets)
+        self._keep = [a]
         h = C.c_void_p()
-        check(self.lib.scft_batch_create(arr, self.count, C.byref(h)), "scft_batch_create")
+        check(self.lib.scft_batch_create(C.cast(desc.ctypes.data, C.POINTER(L.ScftInstance)), self.count,
+                                         C.byref(h)), "scft_batch_create")
         self._keep = []
         self.h = h
+
+    @classmethod
+    def from_arrays(cls, arrays):
+        return cls(arrays=arrays)
+
+    @staticmethod
+    def pack(instances):
+        """Per-instance dicts -> dict of host arrays: n_nodes, L, nsteps, ds, rule
+        (one entry per instance) and x, f0, w0 (node arrays concatenated; x and
+        w0 may be None, then the library uses a uniform mesh on [0, L] and a zero
+        field)."""
+        n = np.array([int(d["n_nodes"]) for d in instances], dtype=np.int64)
+        out = {"n_nodes": n,
+               "L": np.array([float(d.get("L", 0.0)) for d in instances]),
+               "nsteps": np.array([int(d["nsteps"]) for d in instances], dtype=np.int32),
+               "ds": np.array([float(d["ds"]) for d in instances]),
+               "rule": np.array([int(d.get("rule", L.RULE_ROMBERG)) for d in instances], dtype=np.int32)}
+        for key in ("x", "f0", "w0"):
+            have = [d.get(key) is not None for d in instances]
+            if key == "f0" and not all(have):
+                raise ValueError("every instance needs f0")
+            if not any(have):
+                out[key] = None
+                continue
+            if not all(have):
+                raise ValueError(f"{key}: give it for every instance or for none")
+            parts = [np.asarray(d[key], dtype=np.float64) for d in instances]
+            if any(p.shape != (k,) for p, k in zip(parts, n)):
+                raise ValueError(f"{key}: every array needs n_nodes entries")
+            out[key] = np.ascontiguousarray(np.concatenate(parts))
+        return out
+
+    @staticmethod
+    def _descriptors(a, offsets):
+        """The scft_instance array as a numpy structured array with the C layout
+        (field offsets of the ctypes mirror), pointing into the packed arrays."""
+        st = L.ScftInstance
+        names = [f for f, _ in st._fields_]
+        fmt = {"n_nodes": np.int32, "x": np.uint64, "L": np.float64, "f0": np.uint64, "w0": np.uint64,
+               "nsteps": np.int32, "ds": np.float64, "rule": np.int32}
+        dt = np.dtype({"names": names, "formats": [fmt[f] for f in names],
+                       "offsets": [getattr(st, f).offset for f in names], "itemsize": C.sizeof(st)})
+        cnt = len(a["n_nodes"])
+        desc = np.zeros(cnt, dtype=dt)
+        for k in ("n_nodes", "L", "nsteps", "ds", "rule"):
+            desc[k] = a[k]
+        total = int(offsets[-1])
+        for key in ("x", "f0", "w0"):
+            arr = a[key]
+            if arr is None:
+                continue
+            if arr.dtype != np.float64 or not arr.flags.c_contiguous or arr.size != total:
+                raise ValueError(f"{key}: need {total} contiguous doubles")
+            desc[key] = (arr.ctypes.data + 8 * offsets[:-1]).astype(np.uint64)
+        return desc
 
     def split(self, flat):
         return [flat[self.offsets[i]:self.offsets[i + 1]] for i in range(self.count)]

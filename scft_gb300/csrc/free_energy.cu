@@ -10,6 +10,7 @@
 
 #include "batch.cuh"
 #include "common.cuh"
+#include "memory.cuh"
 #include "scft.h"
 
 namespace {
@@ -74,9 +75,9 @@ extern "C" int scft_batch_free_energy(scft_batch *b, int m, const double *f0_sam
     return scft_internal_set_error(SCFT_EINVAL, "scft_batch_free_energy: m must be a power of two >= 16");
   const size_t ns = (size_t)b->count * (m + 1);
   double *d_f = nullptr, *d_F = nullptr, *d_qw = nullptr;
-  cudaError_t e = cudaMalloc(&d_f, ns * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&d_F, b->count * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&d_qw, 16 * sizeof(double));
+  cudaError_t e = scft::mem_alloc((void **)&d_f, ns * sizeof(double));
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&d_F, b->count * sizeof(double));
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&d_qw, 16 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_f, f0_samples, ns * sizeof(double), cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_qw, qw, 16 * sizeof(double), cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess) {
@@ -87,9 +88,9 @@ extern "C" int scft_batch_free_energy(scft_batch *b, int m, const double *f0_sam
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(F, d_F, b->count * sizeof(double), cudaMemcpyDeviceToHost, b->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-  cudaFree(d_f);
-  cudaFree(d_F);
-  cudaFree(d_qw);
+  scft::mem_free(d_f);
+  scft::mem_free(d_F);
+  scft::mem_free(d_qw);
   if (e != cudaSuccess) return scft_internal_set_error(SCFT_ECUDA, cudaGetErrorString(e));
   return SCFT_OK;
 }

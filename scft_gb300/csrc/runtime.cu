@@ -24,6 +24,7 @@
 #include "mixing.cuh"
 #include "batch.cuh"
 #include "propagate_launch.cuh"
+#include "memory.cuh"
 #include "scft.h"
 
 namespace scft {
@@ -111,16 +112,16 @@ template <typename T>
 static int dalloc(T **p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  cudaError_t e = mem_alloc((void **)p, n * sizeof(T));
   if (e != cudaSuccess) {
     *p = nullptr;
-    return set_err(SCFT_ENOMEM, "cudaMalloc(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
+    return set_err(SCFT_ENOMEM, "device allocation of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
   }
   return SCFT_OK;
 }
 template <typename T>
 static void dfree(T *&p) {
-  if (p) cudaFree((void *)p);
+  if (p) mem_free((void *)p);
   p = nullptr;
 }
 
@@ -225,7 +226,7 @@ BatchDev batch_dev(const scft_batch *B) {
 static void free_plans(scft_batch *B, int p) {
   for (auto &c : B->plans[p]) {
     dfree(c.d_items);
-    if (c.scratch) cudaFree(c.scratch);
+    if (c.scratch) mem_free(c.scratch);
     c.scratch = nullptr;
   }
   B->plans[p].clear();
@@ -289,7 +290,7 @@ static int plan(scft_batch *B, int p, double frac) {
     c.slot_elems = (long long)(maxhalf + 1) * 32 * c.NW * c.C;
     const size_t esz = (p == PREC_F32) ? 4 : 8;
     for (;;) {
-      cudaError_t e = cudaMalloc(&c.scratch, (size_t)c.workers * c.slot_elems * esz);
+      cudaError_t e = mem_alloc(&c.scratch, (size_t)c.workers * c.slot_elems * esz);
       if (e == cudaSuccess) break;
       cudaGetLastError();
       c.scratch = nullptr;
@@ -369,12 +370,12 @@ static int live_prepare(scft_batch *B, int K) {
   const int maxc = (int)std::max<size_t>(1, std::max(B->plans[0].size(), B->plans[1].size()));
   const int need = K * 2 * maxc;
   if (need > B->live_cap) {
-    if (B->d_work) cudaFree(B->d_work);
-    if (B->h_work) cudaFreeHost(B->h_work);
+    if (B->d_work) mem_free(B->d_work);
+    if (B->h_work) host_free(B->h_work);
     B->d_work = nullptr;
     B->h_work = nullptr;
-    CK(cudaMalloc(&B->d_work, need * sizeof(unsigned long long)));
-    CK(cudaMallocHost(&B->h_work, need * sizeof(unsigned long long)));
+    CK(mem_alloc((void **)&B->d_work, need * sizeof(unsigned long long)));
+    CK(host_alloc((void **)&B->h_work, need * sizeof(unsigned long long)));
     while ((int)B->ev_live.size() < 2 * need) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e));
@@ -449,7 +450,7 @@ static void free_mix(scft_batch *B) {
   dfree(B->d_hdx); dfree(B->d_hdg); dfree(B->d_gram); dfree(B->d_err); dfree(B->d_best); dfree(B->d_lk);
   dfree(B->d_ref_err); dfree(B->d_ref_it);
   dfree(B->d_iters); dfree(B->d_hcount); dfree(B->d_hhead); dfree(B->d_nactive);
-  if (B->h_nactive) cudaFreeHost(B->h_nactive);
+  if (B->h_nactive) host_free(B->h_nactive);
   B->h_nactive = nullptr;
   B->depth = 0;
 }
@@ -466,7 +467,7 @@ static int ensure_mix(scft_batch *B, int depth) {
       (rc = dalloc(&B->d_hcount, c)) || (rc = dalloc(&B->d_hhead, c)) || (rc = dalloc(&B->d_nactive, 1)) ||
       (rc = dalloc(&B->d_ref_err, c)) || (rc = dalloc(&B->d_ref_it, c)))
     return rc;
-  CK(cudaMallocHost(&B->h_nactive, sizeof(int)));
+  CK(host_alloc((void **)&B->h_nactive, sizeof(int)));
   B->depth = depth;
   return SCFT_OK;
 }
@@ -486,8 +487,8 @@ static void destroy_batch(scft_batch *B) {
   for (auto s : B->side) cudaStreamDestroy(s);
   for (auto e : B->ev_join) cudaEventDestroy(e);
   for (auto e : B->ev_live) cudaEventDestroy(e);
-  if (B->d_work) cudaFree(B->d_work);
-  if (B->h_work) cudaFreeHost(B->h_work);
+  if (B->d_work) mem_free(B->d_work);
+  if (B->h_work) host_free(B->h_work);
   if (B->ev_fork) cudaEventDestroy(B->ev_fork);
   if (B->st) cudaStreamDestroy(B->st);
   delete B;
@@ -530,18 +531,6 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
     no += s.n_nodes; io += s.n_nodes - 2;
   }
   B->total_nodes = no; B->total_int = io;
-  std::vector<double> hx(no), hf(no), hw(no), hqw(16 * (size_t)count);
-  for (int i = 0; i < count; i++) {
-    const scft_instance &s = inst[i];
-    double *x = hx.data() + B->node_off[i];
-    for (int k = 0; k < s.n_nodes; k++) {
-      x[k] = s.x ? s.x[k] : s.L * (double)k / (double)(s.n_nodes - 1);
-      hf[B->node_off[i] + k] = s.f0[k];
-      hw[B->node_off[i] + k] = s.w0 ? s.w0[k] : 0.0;
-    }
-    if (!s.x) x[s.n_nodes - 1] = s.L;
-    quad_table(s.nsteps, s.ds, s.rule, hqw.data() + 16 * (size_t)i);
-  }
   int rc;
   if ((rc = dalloc(&B->d_n, count)) || (rc = dalloc(&B->d_nsteps, count)) || (rc = dalloc(&B->d_active, count)) ||
       (rc = dalloc(&B->d_status, count)) || (rc = dalloc(&B->d_ds, count)) || (rc = dalloc(&B->d_x, no)) ||
@@ -558,26 +547,59 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
     destroy_batch(B);
     return set_err(SCFT_ECUDA, "event creation failed");
   }
+  // one pinned staging buffer (from the library's cache) for every upload
+  const size_t nd = (size_t)no, nc = (size_t)count;
+  const size_t stage_doubles = 3 * nd + 16 * nc + nc + 2 * nc + nc;  // x, f0, w | qw | ds | offsets | n+nsteps
+  double *stage = nullptr;
+  if (host_alloc((void **)&stage, stage_doubles * sizeof(double)) != cudaSuccess) {
+    destroy_batch(B);
+    return set_err(SCFT_ENOMEM, "pinned staging buffer of %zu bytes", stage_doubles * sizeof(double));
+  }
+  double *hx = stage, *hf = hx + nd, *hw = hf + nd, *hqw = hw + nd, *hds = hqw + 16 * nc;
+  long long *hno = reinterpret_cast<long long *>(hds + nc), *hio = hno + nc;
+  int *hn = reinterpret_cast<int *>(hio + nc), *hns = hn + nc;
+  for (int i = 0; i < count; i++) {
+    const scft_instance &s = inst[i];
+    const long long o = B->node_off[i];
+    for (int k = 0; k < s.n_nodes; k++) {
+      hx[o + k] = s.x ? s.x[k] : s.L * (double)k / (double)(s.n_nodes - 1);
+      hf[o + k] = s.f0[k];
+      hw[o + k] = s.w0 ? s.w0[k] : 0.0;
+    }
+    if (!s.x) hx[o + s.n_nodes - 1] = s.L;
+    quad_table(s.nsteps, s.ds, s.rule, hqw + 16 * (size_t)i);
+    hds[i] = s.ds;
+    hno[i] = o;
+    hio[i] = B->int_off[i];
+    hn[i] = s.n_nodes;
+    hns[i] = s.nsteps;
+  }
   cudaStream_t st = B->st;
   struct Cp { void *d; const void *h; size_t bytes; } cps[] = {
-      {B->d_n, B->n.data(), count * sizeof(int)},
-      {B->d_nsteps, B->nsteps.data(), count * sizeof(int)},
-      {B->d_ds, B->ds.data(), count * sizeof(double)},
-      {B->d_node_off, B->node_off.data(), count * sizeof(long long)},
-      {B->d_int_off, B->int_off.data(), count * sizeof(long long)},
-      {B->d_x, hx.data(), no * sizeof(double)},
-      {B->d_f0, hf.data(), no * sizeof(double)},
-      {B->d_w, hw.data(), no * sizeof(double)},
-      {B->d_w0, hw.data(), no * sizeof(double)},
-      {B->d_qw, hqw.data(), hqw.size() * sizeof(double)},
+      {B->d_n, hn, nc * sizeof(int)},
+      {B->d_nsteps, hns, nc * sizeof(int)},
+      {B->d_ds, hds, nc * sizeof(double)},
+      {B->d_node_off, hno, nc * sizeof(long long)},
+      {B->d_int_off, hio, nc * sizeof(long long)},
+      {B->d_x, hx, nd * sizeof(double)},
+      {B->d_f0, hf, nd * sizeof(double)},
+      {B->d_w, hw, nd * sizeof(double)},
+      {B->d_w0, hw, nd * sizeof(double)},
+      {B->d_qw, hqw, 16 * nc * sizeof(double)},
   };
   for (auto &c : cps) {
     cudaError_t e = cudaMemcpyAsync(c.d, c.h, c.bytes, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) { destroy_batch(B); return set_err(SCFT_ECUDA, "upload: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(st);
+      host_free(stage);
+      destroy_batch(B);
+      return set_err(SCFT_ECUDA, "upload: %s", cudaGetErrorString(e));
+    }
   }
   cudaMemsetAsync(B->d_status, 0, count * sizeof(int), st);
   cudaMemsetAsync(B->d_phi, 0, no * sizeof(double), st);
   cudaError_t e = cudaStreamSynchronize(st);
+  host_free(stage);
   if (e != cudaSuccess) { destroy_batch(B); return set_err(SCFT_ECUDA, "upload: %s", cudaGetErrorString(e)); }
   *out = B;
   return SCFT_OK;
@@ -1255,7 +1277,7 @@ int scft_set_config(const scft_config *c) {
   DropIn &D = g_drop;
   if (D.B) { destroy_batch(D.B); D.B = nullptr; }
   dfree(D.d_in); dfree(D.d_out);
-  if (D.h_stage) cudaFreeHost(D.h_stage);
+  if (D.h_stage) host_free(D.h_stage);
   D.h_stage = nullptr;
   D.set = false;
   D.n = c->n_nodes; D.nsteps = c->nsteps; D.ds = c->ds; D.rule = c->rule;
@@ -1272,7 +1294,7 @@ int scft_set_config(const scft_config *c) {
   if (rc) return rc;
   if ((rc = plan(D.B, D.prec, 1.0))) return rc;
   if ((rc = dalloc(&D.d_in, D.n)) || (rc = dalloc(&D.d_out, D.n))) return rc;
-  CK(cudaMallocHost(&D.h_stage, 2 * D.n * sizeof(double)));
+  CK(host_alloc((void **)&D.h_stage, 2 * D.n * sizeof(double)));
   D.set = true;
   return SCFT_OK;
 }

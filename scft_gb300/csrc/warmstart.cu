@@ -19,6 +19,7 @@
 
 #include "batch.cuh"
 #include "common.cuh"
+#include "memory.cuh"
 #include "scft.h"
 
 namespace scft {
@@ -278,18 +279,18 @@ static int ws_err(int code, const char *msg);
 
 static int ws_reserve(scft_ws *W, int B) {
   if (B <= W->cap) return SCFT_OK;
-  cudaFree(W->d_feat); cudaFree(W->d_tgt); cudaFree(W->d_out); cudaFree(W->d_gout);
-  for (auto &a : W->d_act) cudaFree(a);
-  cudaFree(W->d_ga); cudaFree(W->d_gb); cudaFree(W->d_idx);
+  scft::mem_free(W->d_feat); scft::mem_free(W->d_tgt); scft::mem_free(W->d_out); scft::mem_free(W->d_gout);
+  for (auto &a : W->d_act) scft::mem_free(a);
+  scft::mem_free(W->d_ga); scft::mem_free(W->d_gb); scft::mem_free(W->d_idx);
   const size_t P = WS_P, esz = W->bf16 ? 2 : 4;
-  WCK(cudaMalloc(&W->d_feat, sizeof(float) * B * WS_IN * P));
-  WCK(cudaMalloc(&W->d_tgt, sizeof(float) * B * P));
-  WCK(cudaMalloc(&W->d_out, sizeof(float) * B * P));
-  WCK(cudaMalloc(&W->d_gout, sizeof(float) * B * P));
-  for (auto &a : W->d_act) WCK(cudaMalloc(&a, esz * B * 64 * P));
-  WCK(cudaMalloc(&W->d_ga, sizeof(float) * B * 64 * P));
-  WCK(cudaMalloc(&W->d_gb, sizeof(float) * B * 64 * P));
-  WCK(cudaMalloc(&W->d_idx, sizeof(int) * B));
+  WCK(scft::mem_alloc((void **)&W->d_feat, sizeof(float) * B * WS_IN * P));
+  WCK(scft::mem_alloc((void **)&W->d_tgt, sizeof(float) * B * P));
+  WCK(scft::mem_alloc((void **)&W->d_out, sizeof(float) * B * P));
+  WCK(scft::mem_alloc((void **)&W->d_gout, sizeof(float) * B * P));
+  for (auto &a : W->d_act) WCK(scft::mem_alloc((void **)&a, esz * B * 64 * P));
+  WCK(scft::mem_alloc((void **)&W->d_ga, sizeof(float) * B * 64 * P));
+  WCK(scft::mem_alloc((void **)&W->d_gb, sizeof(float) * B * 64 * P));
+  WCK(scft::mem_alloc((void **)&W->d_idx, sizeof(int) * B));
   W->cap = B;
   return SCFT_OK;
 }
@@ -405,12 +406,12 @@ int scft_ws_create(int act_bf16, unsigned long long seed, scft_ws **out) {
     for (int i = 0; i < kLayers[l].co * kLayers[l].ci * WS_K; i++) h[W->poff[l] + i] = (float)U(rng);
   }
   cudaError_t e = cudaStreamCreateWithFlags(&W->st, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&W->d_p, sizeof(float) * off);
-  if (e == cudaSuccess) e = cudaMalloc(&W->d_g, sizeof(float) * off);
-  if (e == cudaSuccess) e = cudaMalloc(&W->d_m, sizeof(float) * off);
-  if (e == cudaSuccess) e = cudaMalloc(&W->d_v, sizeof(float) * off);
-  if (e == cudaSuccess) e = cudaMalloc(&W->d_wt, sizeof(float) * 64 * 64 * WS_K);
-  if (e == cudaSuccess) e = cudaMalloc(&W->d_loss, sizeof(double) * 65536);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_p, sizeof(float) * off);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_g, sizeof(float) * off);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_m, sizeof(float) * off);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_v, sizeof(float) * off);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_wt, sizeof(float) * 64 * 64 * WS_K);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_loss, sizeof(double) * 65536);
   if (e == cudaSuccess) e = cudaMemcpy(W->d_p, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(W->d_m, 0, sizeof(float) * off);
   if (e == cudaSuccess) e = cudaMemset(W->d_v, 0, sizeof(float) * off);
@@ -425,10 +426,10 @@ int scft_ws_create(int act_bf16, unsigned long long seed, scft_ws **out) {
 int scft_ws_destroy(scft_ws *W) {
   if (!W) return SCFT_OK;
   if (W->st) cudaStreamSynchronize(W->st);
-  cudaFree(W->d_p); cudaFree(W->d_g); cudaFree(W->d_m); cudaFree(W->d_v); cudaFree(W->d_wt);
-  cudaFree(W->d_loss); cudaFree(W->d_feat); cudaFree(W->d_tgt); cudaFree(W->d_out); cudaFree(W->d_gout);
-  for (auto &a : W->d_act) cudaFree(a);
-  cudaFree(W->d_ga); cudaFree(W->d_gb); cudaFree(W->d_idx); cudaFree(W->d_dsf); cudaFree(W->d_dst);
+  scft::mem_free(W->d_p); scft::mem_free(W->d_g); scft::mem_free(W->d_m); scft::mem_free(W->d_v); scft::mem_free(W->d_wt);
+  scft::mem_free(W->d_loss); scft::mem_free(W->d_feat); scft::mem_free(W->d_tgt); scft::mem_free(W->d_out); scft::mem_free(W->d_gout);
+  for (auto &a : W->d_act) scft::mem_free(a);
+  scft::mem_free(W->d_ga); scft::mem_free(W->d_gb); scft::mem_free(W->d_idx); scft::mem_free(W->d_dsf); scft::mem_free(W->d_dst);
   if (W->st) cudaStreamDestroy(W->st);
   delete W;
   return SCFT_OK;
@@ -479,16 +480,16 @@ int scft_ws_loss_grad(scft_ws *W, const float *features, const float *targets, i
 int scft_ws_batch_features(scft_batch *b, float *features, float *targets) {
   if (!b || !features) return ws_err(SCFT_EINVAL, "scft_ws_batch_features");
   float *df = nullptr, *dt = nullptr;
-  WCK(cudaMalloc(&df, sizeof(float) * b->count * WS_IN * WS_P));
-  if (targets) WCK(cudaMalloc(&dt, sizeof(float) * b->count * WS_P));
+  WCK(scft::mem_alloc((void **)&df, sizeof(float) * b->count * WS_IN * WS_P));
+  if (targets) WCK(scft::mem_alloc((void **)&dt, sizeof(float) * b->count * WS_P));
   features_kernel<<<b->count, WS_P, 0, b->st>>>(ws_view(b), nullptr, b->count, df, dt);
   scft_count_launches(1);
   WCK(cudaGetLastError());
   WCK(cudaMemcpyAsync(features, df, sizeof(float) * b->count * WS_IN * WS_P, cudaMemcpyDeviceToHost, b->st));
   if (targets) WCK(cudaMemcpyAsync(targets, dt, sizeof(float) * b->count * WS_P, cudaMemcpyDeviceToHost, b->st));
   WCK(cudaStreamSynchronize(b->st));
-  cudaFree(df);
-  cudaFree(dt);
+  scft::mem_free(df);
+  scft::mem_free(dt);
   return SCFT_OK;
 }
 
@@ -501,9 +502,9 @@ int scft_ws_dataset_from_batch(scft_ws *W, scft_batch *b, const int *mask) {
   const int n = (int)sel.size(), old = W->nds;
   float *nf = nullptr, *nt = nullptr;
   int *ds = nullptr;
-  WCK(cudaMalloc(&nf, sizeof(float) * (size_t)(old + n) * WS_IN * WS_P));
-  WCK(cudaMalloc(&nt, sizeof(float) * (size_t)(old + n) * WS_P));
-  WCK(cudaMalloc(&ds, sizeof(int) * n));
+  WCK(scft::mem_alloc((void **)&nf, sizeof(float) * (size_t)(old + n) * WS_IN * WS_P));
+  WCK(scft::mem_alloc((void **)&nt, sizeof(float) * (size_t)(old + n) * WS_P));
+  WCK(scft::mem_alloc((void **)&ds, sizeof(int) * n));
   if (old) {
     WCK(cudaMemcpyAsync(nf, W->d_dsf, sizeof(float) * (size_t)old * WS_IN * WS_P, cudaMemcpyDeviceToDevice, b->st));
     WCK(cudaMemcpyAsync(nt, W->d_dst, sizeof(float) * (size_t)old * WS_P, cudaMemcpyDeviceToDevice, b->st));
@@ -513,9 +514,9 @@ int scft_ws_dataset_from_batch(scft_ws *W, scft_batch *b, const int *mask) {
   scft_count_launches(1);
   WCK(cudaGetLastError());
   WCK(cudaStreamSynchronize(b->st));
-  cudaFree(ds);
-  cudaFree(W->d_dsf);
-  cudaFree(W->d_dst);
+  scft::mem_free(ds);
+  scft::mem_free(W->d_dsf);
+  scft::mem_free(W->d_dst);
   W->d_dsf = nf;
   W->d_dst = nt;
   W->nds = old + n;
@@ -532,7 +533,7 @@ int scft_ws_train(scft_ws *W, int steps, int batch, float lr, unsigned long long
   for (int i = 0; i < W->nds; i++) perm[i] = i;
   size_t pos = W->nds;
   int *h_idx = nullptr;
-  WCK(cudaMallocHost(&h_idx, sizeof(int) * batch * 2));
+  WCK(scft::host_alloc((void **)&h_idx, sizeof(int) * batch * 2));
   WCK(cudaMemsetAsync(W->d_loss, 0, sizeof(double) * steps, W->st));
   const float b1 = 0.9f, b2 = 0.999f;
   for (int s = 0; s < steps; s++) {
@@ -547,7 +548,7 @@ int scft_ws_train(scft_ws *W, int steps, int batch, float lr, unsigned long long
     gather_rows_kernel<<<(unsigned)((nf + 255) / 256), 256, 0, W->st>>>(W->d_dsf, W->d_idx, batch, WS_IN * WS_P, W->d_feat);
     gather_rows_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, W->st>>>(W->d_dst, W->d_idx, batch, WS_P, W->d_tgt);
     scft_count_launches(2);
-    if ((rc = ws_forward(W, batch)) || (rc = ws_backward(W, batch, s))) { cudaFreeHost(h_idx); return rc; }
+    if ((rc = ws_forward(W, batch)) || (rc = ws_backward(W, batch, s))) { scft::host_free(h_idx); return rc; }
     W->adam_t++;
     const float c1 = 1.f - std::pow(b1, (float)W->adam_t), c2 = 1.f - std::pow(b2, (float)W->adam_t);
     // cosine decay from lr to lr/50 over the run
@@ -558,7 +559,7 @@ int scft_ws_train(scft_ws *W, int steps, int batch, float lr, unsigned long long
     WCK(cudaGetLastError());
   }
   WCK(cudaStreamSynchronize(W->st));
-  cudaFreeHost(h_idx);
+  scft::host_free(h_idx);
   if (losses) {
     std::vector<double> l(steps);
     WCK(cudaMemcpy(l.data(), W->d_loss, sizeof(double) * steps, cudaMemcpyDeviceToHost));

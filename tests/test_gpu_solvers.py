@@ -240,3 +240,19 @@ def test_stalled_fp32_instances_finish_in_fp64():
         b.reset()
         r = b.solve(api.solve_opts(precision=F32, tol=1e-6, finish_stall=0))
         assert not np.any(r["status"] & 64)
+
+
+def test_released_memory_is_reused_and_trimmed(lib):
+    """Batches release their device blocks into the library's cache; the next
+    batch of the same shape reuses them (same results) and scft_mem_trim hands
+    the cached blocks back to CUDA."""
+    insts = W.batch_mixed(16, seed=90)
+    outs = []
+    for _ in range(2):
+        with api.Batch(insts) as b:
+            b.evaluate(F32)
+            outs.append(b.get()[1])
+    for a, c in zip(*outs):
+        np.testing.assert_array_equal(a, c)
+    assert lib.scft_mem_trim() > 0
+    assert lib.scft_mem_trim() == 0
