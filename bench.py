@@ -206,11 +206,12 @@ def cpu_sample(insts, target):
     return insts[::stride][:target]
 
 
-def run_cpu(sample, workers=None):
+def run_cpu(sample, workers=None, **kw):
     from oracle import oracle as orc
 
     orc.build(with_reference=False)
-    out, dt, nw = orc.cpu_solve_batch(sample, workers=workers, tol=TOL)
+    kw.setdefault("tol", TOL)
+    out, dt, nw = orc.cpu_solve_batch(sample, workers=workers, **kw)
     conv = sum(1 for rc, _, _ in out if rc == 0)
     return conv, dt, nw, out
 
@@ -424,6 +425,9 @@ def ours_arm(args):
                        "host_ms": {k: 1e3 * statistics.mean(p[i] for p in parts)
                                    for i, k in enumerate(("create_and_upload", "warm_start_and_solve", "download"))}}
 
+    if rank == 0 and world == 1 and not args.no_configs:
+        line["configs"] = config_legs(ws)
+
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = cpu_sample(mine, args.cpu_sample)
         conv_c, dt, nw, _ = run_cpu(sample)
@@ -436,6 +440,101 @@ def ours_arm(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def config_legs(ws):
+    """The workload configs other than the headline batch, each on its own
+    scale, run after the timed region: the CPU-runnable single instance
+    (33 nodes, FP64 to 1e-8, beta 0.1), the 1024-element FP32-vs-FP64 error
+    report, the autotuned 4096-instance mixed batch and the propagator pass of
+    the graded 8192-element workload."""
+    import torch
+
+    from scft_gb300 import F32, F64, ST_CONVERGED, api
+    from scft_gb300 import workloads as W
+
+    out = {}
+    # 33 nodes, 2048 steps, L = 4: FP64 throughout, Anderson depth 10 and beta 0.1, tol 1e-8
+    d = W.single_small()
+    o1 = api.solve_opts(precision=F64, tol=1e-8, beta=0.1, maxit=5000)
+    with api.Batch([d]) as b:
+        b.solve(o1)
+        b.reset()
+        r = b.solve(o1)
+        ms = b.last_ms()
+    c1 = {"workload": "33 nodes (32 elements), L = 4, 2048 steps, FP64, Anderson depth 10, beta 0.1, tol 1e-8",
+          "gpu_ms": ms, "iterations": int(r["iterations"][0]), "err": float(r["err"][0]),
+          "converged": bool(r["status"][0] & ST_CONVERGED)}
+    conv, dt, nw, res = run_cpu([dict(d, rule=d.get("rule", 0))], workers=1, tol=1e-8, beta=0.1, maxit=5000)
+    c1["cpu_baseline"] = {"ms": 1e3 * dt, "iterations": int(res[0][1]), "cores": 1, "kind": "port"}
+    out["single_small_fp64"] = c1
+
+    # 1024 elements, 2048 steps: FP32 converged field vs the FP64 one
+    d = W.single_large()
+    m = 2 ** 14
+    xs = np.linspace(0.0, d["L"], m + 1)
+    fs = W.gauss_wall_f0(xs, d["L"])[None, :]
+    c2 = {"workload": "1025 nodes, L = 4, 2048 steps, single instance, tol 1e-6"}
+    with api.Batch([d]) as b:
+        for prec, tag in ((F64, "fp64"), (F32, "fp32")):
+            b.reset()
+            r = b.solve(api.solve_opts(precision=prec, tol=1e-6))
+            c2[tag + "_ms"] = b.last_ms()
+            c2[tag + "_iterations"] = int(r["iterations"][0])
+            w, phi, Q = b.get()
+            c2[tag] = (w[0], phi[0], Q[0], float(b.free_energy(fs)[0]))
+        b.set_fields([c2["fp32"][0]])
+        b.evaluate(F64)
+        _, phi64_at32, _ = b.get()
+    w64, p64, q64, f64 = c2.pop("fp64")
+    w32, p32, q32, f32 = c2.pop("fp32")
+    c2.update(phi_err_vs_fp64=float(np.abs(p32 - p64).max()), Q_rel_err=abs(q32 - q64) / abs(q64),
+              free_energy_err=abs(f32 - f64), free_energy_fp64=f64,
+              fp32_field_fp64_residual=float(np.abs(phi64_at32[0][1:-1] - d["f0"][1:-1]).max()))
+    out["single_large_fp32_vs_fp64"] = c2
+
+    # 4096 mixed instances, cold start, autotuned shapes
+    insts = W.batch_mixed(4096)
+    with api.Batch(insts) as b:
+        t = time.perf_counter()
+        b.autotune(F32)
+        tune_s = time.perf_counter() - t
+        o3 = api.solve_opts(precision=F32, tol=1e-6)
+        b.reset(); b.solve(o3)
+        ts, convs = [], []
+        for _ in range(2):
+            b.reset()
+            r = b.solve(o3)
+            ts.append(b.last_ms())
+            convs.append(int(((r["status"] & ST_CONVERGED) != 0).sum()))
+        out["batch_mixed"] = {"workload": "4096 instances, elements log-uniform in [32, 1024], L ~ U[2, 10], "
+                                          "steps in {512, 1024, 2048, 4096}, cold start, FP32 propagator",
+                              "value": convs[-1] / (statistics.mean(ts) / 1e3), "unit": UNIT,
+                              "ms": statistics.mean(ts), "converged": convs[-1], "autotune_s": tune_s,
+                              "iterations_mean": float(r["iterations"].mean()), "iterations_max": int(r["iterations"].max()),
+                              "classes": [(c["C"], c["NW"]) for c in b.profile(F32)]}
+
+    # graded 8192-element meshes, 8192 steps: one propagator pass (the q-slice stream)
+    insts = W.batch_graded(64)
+    alg = sum(2.0 * 4 * dd["n_nodes"] * (dd["nsteps"] // 2 + 1) for dd in insts)
+    with api.Batch(insts) as b:
+        b.evaluate(F32)
+        t32 = []
+        for _ in range(3):
+            b.evaluate(F32)
+            t32.append(b.last_ms())
+        ms32 = min(t32)
+        b.evaluate(F64)
+        ms64 = b.last_ms()
+    peak, kind = peaks()
+    out["batch_graded_pass"] = {"workload": "64 instances of the 512-instance graded workload: 8192 elements graded by "
+                                            "1.002 toward both walls, 8192 steps, one propagator pass",
+                                "fp32_ms": ms32, "fp64_ms": ms64, "alg_bytes_fp32": alg,
+                                "alg_GBps_fp32": alg / (ms32 / 1e3) / 1e9, "frac_of_peak": alg / (ms32 / 1e3) / 1e9 / peak,
+                                "peak_source": kind,
+                                "solve": "not run: the batched mixing does not converge on meshes graded to h_min ~ 1e-6"}
+    torch.cuda.synchronize()
+    return out
 
 
 def profile_pass(args):
@@ -471,6 +570,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other workload configs")
     ap.add_argument("--profile-pass", action="store_true", help="one FP32 propagator pass (for ncu)")
     args = ap.parse_args()
     if args.profile_pass:

@@ -37,6 +37,8 @@ extern "C" {
 enum { SCFT_RULE_ROMBERG = 0, SCFT_RULE_TRAPEZOID = 1 };
 enum { SCFT_F32 = 0, SCFT_F64 = 1 };
 enum { SCFT_MIX_LINEAR = 0, SCFT_MIX_LOG = 1 };
+enum { SCFT_SCHEME_IE = 0, SCFT_SCHEME_IRK2 = 1 };   /* implicit Euler (1D_FEM.c) | Gauss-Legendre IRK2 (drivescft.cc) */
+enum { SCFT_W_ROWSCALED = 0, SCFT_W_CONSISTENT = 1 }; /* W_ij = w_i M_ij (1D_FEM.c:104) | int w_h phi_i phi_j (scft.cc:653) */
 
 /* =========================================================================
  * Drop-in single-instance path (the reference's process globals become one
@@ -53,6 +55,12 @@ typedef struct scft_config {
   int rule;          /* SCFT_RULE_ROMBERG (romint.c:21) or SCFT_RULE_TRAPEZOID (.m:119-124) */
   int sign;          /* +1: out = phi - f0 (1D_FEM.c:276); -1: out = f0 - phi (drivescft.cc:212) */
   int precision;     /* SCFT_F64 (default) or SCFT_F32 */
+  int scheme;        /* SCFT_SCHEME_IE (default, 1D_FEM.c:208-228) or SCFT_SCHEME_IRK2 (the 2-stage
+                        Gauss-Legendre method of drivescft.cc:130-165; FP64 only) */
+  int wmode;         /* SCFT_W_ROWSCALED (default, 1D_FEM.c:104-105) or SCFT_W_CONSISTENT
+                        (scft.cc:653-655; FP64 only) */
+  double w_wall[2];  /* field at nodes 0 and n-1, used by the consistent field term (the deal.II
+                        field files carry wall values); 0 by default */
 } scft_config;
 
 /* Defaults of the drop-in: 2049 steps of ds = 1/2048 with the trapezoid rule
@@ -322,6 +330,14 @@ int scft_res_read(const char *path, int max_rows, int *rows, double *table, int 
    retries.  This returns the cached blocks of the current device and the cached
    pinned blocks to CUDA and reports the bytes released. */
 long long scft_mem_trim(void);
+
+/* Density and Q of every instance of b (FP64) with the given contour scheme and
+   field term: SCFT_SCHEME_IRK2 with SCFT_W_CONSISTENT is the propagator of the
+   reference's deal.II driver (drivescft.cc:130-207, scft.cc:589-696);
+   SCFT_SCHEME_IE with SCFT_W_ROWSCALED is the one of 1D_FEM.c.  Results via
+   scft_batch_get; one thread per instance (complex Thomas sweeps of the
+   decoupled stage system).  No counterpart of its own in the reference. */
+int scft_batch_evaluate_scheme(scft_batch *b, int scheme, int wmode);
 
 /* Kernels launched by this library since load (graph replays count each node). */
 long long scft_kernel_launches(void);

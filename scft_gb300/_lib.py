@@ -29,6 +29,8 @@ ST_WATCHDOG = 32
 
 RULE_ROMBERG, RULE_TRAPEZOID = 0, 1
 F32, F64 = 0, 1
+SCHEME_IE, SCHEME_IRK2 = 0, 1
+W_ROWSCALED, W_CONSISTENT = 0, 1
 MIX_LINEAR, MIX_LOG = 0, 1
 
 _dp = C.POINTER(C.c_double)
@@ -40,7 +42,7 @@ VECFUNC = C.CFUNCTYPE(None, C.c_int, _dp, _dp)
 class ScftConfig(C.Structure):
     _fields_ = [("n_nodes", C.c_int), ("x", _dp), ("L", C.c_double), ("f0", _dp),
                 ("nsteps", C.c_int), ("ds", C.c_double), ("rule", C.c_int), ("sign", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("scheme", C.c_int), ("wmode", C.c_int), ("w_wall", C.c_double * 2)]
 
 
 class ScftInstance(C.Structure):
@@ -99,6 +101,7 @@ SIGNATURES = {
     "scft_batch_destroy": (C.c_int, [C.c_void_p]),
     "scft_kernel_launches": (C.c_longlong, []),
     "scft_mem_trim": (C.c_longlong, []),
+    "scft_batch_evaluate_scheme": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "scft_ws_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "scft_ws_destroy": (C.c_int, [C.c_void_p]),
     "scft_ws_param_count": (C.c_int, [C.c_void_p]),

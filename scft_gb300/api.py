@@ -64,9 +64,11 @@ _config_keep: list = []
 
 
 def set_config(f0, L_width=None, x=None, nsteps=2049, ds=1.0 / 2048, rule=L.RULE_TRAPEZOID, sign=1,
-               precision=L.F64):
+               precision=L.F64, scheme=L.SCHEME_IE, wmode=L.W_ROWSCALED, w_wall=(0.0, 0.0)):
     """Configure the problem that simple_FEM_1D_transient evaluates (the reference's
-    globals f0_given, L and total_time_step)."""
+    globals f0_given, L and total_time_step).  scheme=SCHEME_IRK2 with
+    wmode=W_CONSISTENT and the field's wall values selects the deal.II
+    propagator (drivescft.cc:130-165, scft.cc:653-655)."""
     lib = L.load()
     f0 = np.ascontiguousarray(f0, dtype=np.float64)
     xa = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
@@ -81,6 +83,9 @@ def set_config(f0, L_width=None, x=None, nsteps=2049, ds=1.0 / 2048, rule=L.RULE
     cfg.rule = int(rule)
     cfg.sign = int(sign)
     cfg.precision = int(precision)
+    cfg.scheme = int(scheme)
+    cfg.wmode = int(wmode)
+    cfg.w_wall[0], cfg.w_wall[1] = float(w_wall[0]), float(w_wall[1])
     check(lib.scft_set_config(C.byref(cfg)), "scft_set_config")
     _config_keep[:] = [f0, xa]
 
@@ -293,6 +298,11 @@ class Batch:
 
     def evaluate(self, precision=L.F64):
         check(self.lib.scft_batch_evaluate(self.h, int(precision)), "scft_batch_evaluate")
+
+    def evaluate_scheme(self, scheme=L.SCHEME_IRK2, wmode=L.W_CONSISTENT):
+        """FP64 density of every instance with the given contour scheme and field
+        term (IRK2 + consistent: the deal.II propagator)."""
+        check(self.lib.scft_batch_evaluate_scheme(self.h, int(scheme), int(wmode)), "scft_batch_evaluate_scheme")
 
     def solve(self, opts: L.ScftSolveOpts | None = None, **kw):
         o = opts if opts is not None else solve_opts(**kw)

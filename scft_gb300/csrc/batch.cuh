@@ -39,6 +39,9 @@ struct scft_batch {
   double *d_graw = nullptr, *d_gcur = nullptr, *d_gprev = nullptr, *d_wprev = nullptr;
   double *d_hdx = nullptr, *d_hdg = nullptr, *d_gram = nullptr, *d_err = nullptr, *d_best = nullptr;
   double *d_lk = nullptr, *d_ref_err = nullptr;
+  // scratch of the scheme-general propagator (scft_batch_evaluate_scheme)
+  double *d_seq = nullptr;
+  long long *d_seq_off = nullptr;
   int *d_ref_it = nullptr;
   int *d_iters = nullptr, *d_hcount = nullptr, *d_hhead = nullptr, *d_nactive = nullptr;
   int *h_nactive = nullptr;

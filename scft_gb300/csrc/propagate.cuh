@@ -46,6 +46,11 @@ namespace scft {
 #ifndef PACKED_BLOCK
 #define PACKED_BLOCK 1
 #endif
+// Minimum resident CTAs per SM the fused solve kernel is compiled for (its
+// register budget); the planner sizes its grid from the occupancy it gets.
+#ifndef SOLVE_MIN_CTAS
+#define SOLVE_MIN_CTAS 1
+#endif
 
 template <typename R>
 __device__ __forceinline__ R fmaR(R a, R b, R c);
@@ -773,7 +778,8 @@ propagate_kernel(BatchDev b, ClassDev cls) {
 
 // Fused persistent solve of one shape class (see Propagator::solve).
 template <typename R, int C, int NW, bool DELTA>
-__global__ void __launch_bounds__(Propagator<R, C, NW, DELTA>::CTA, 1)
+__global__ void __launch_bounds__(Propagator<R, C, NW, DELTA>::CTA,
+                                  Propagator<R, C, NW, DELTA>::CTA * SOLVE_MIN_CTAS <= 1024 ? SOLVE_MIN_CTAS : 1)
 solve_kernel(BatchDev b, ClassDev cls, MixDev m) {
   using Pp = Propagator<R, C, NW, DELTA>;
   __shared__ GroupSmem<R, NW> sm[Pp::GPC];

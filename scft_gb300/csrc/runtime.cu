@@ -41,6 +41,18 @@ static cudaError_t solve_dispatch(int C, int NW, const BatchDev &b, const ClassD
   return NW <= 4 ? solve_launch_f32_a(C, NW, b, cls, m, grid, st, ctas)
                  : solve_launch_f32_b(C, NW, b, cls, m, grid, st, ctas);
 }
+long long seq_scratch_doubles(int n, int nsteps);
+cudaError_t seq_propagate_launch(const BatchDev &b, int scheme, int wmode, double *scratch, const long long *off,
+                                 cudaStream_t st);
+
+static int solve_ctas_per_sm(int C, int NW) {
+  int n = 0;
+  BatchDev b{};
+  ClassDev c{};
+  MixDev m{};
+  if (solve_dispatch(C, NW, b, c, m, 0, 0, &n) != cudaSuccess) return 0;
+  return n;
+}
 
 static cudaError_t dispatch(int prec, int C, int NW, const BatchDev &b, const ClassDev &cls, int grid,
                             cudaStream_t st, int *ctas, bool *exists) {
@@ -281,7 +293,10 @@ static int plan(scft_batch *B, int p, double frac) {
       cost += (double)B->n[i] * B->nsteps[i];
       maxhalf = std::max(maxhalf, B->nsteps[i] / 2);
     }
-    const int cps = std::max(1, propagate_ctas_per_sm(p, c.C, c.NW));
+    // resident CTAs per SM: FP32 classes may also run as the fused solve kernel,
+    // whose register budget can allow more; size the workers for the larger
+    int cps = std::max(1, propagate_ctas_per_sm(p, c.C, c.NW));
+    if (p == PREC_F32) cps = std::max(cps, solve_ctas_per_sm(c.C, c.NW));
     c.gpc = propagate_groups_per_cta(c.C, c.NW);
     int budget = (int)std::floor(cost / total * frac * cps * sms + 0.5);
     budget = std::max(1, budget);
@@ -473,6 +488,8 @@ static int ensure_mix(scft_batch *B, int depth) {
 }
 
 static void destroy_batch(scft_batch *B) {
+  dfree(B->d_seq);
+  dfree(B->d_seq_off);
   if (!B) return;
   if (B->st) cudaStreamSynchronize(B->st);
   free_plans(B, 0);
@@ -621,6 +638,28 @@ static int evaluate(scft_batch *B, int p) {
   return SCFT_OK;
 }
 
+// Enqueue the scheme-general propagator for the active instances of B on B->st
+// (scratch allocated on first use).
+static int seq_enqueue(scft_batch *B, int scheme, int wmode) {
+  if ((scheme != SCFT_SCHEME_IE && scheme != SCFT_SCHEME_IRK2) ||
+      (wmode != SCFT_W_ROWSCALED && wmode != SCFT_W_CONSISTENT))
+    return set_err(SCFT_EINVAL, "scheme %d / field term %d", scheme, wmode);
+  if (!B->d_seq) {
+    std::vector<long long> off(B->count);
+    long long tot = 0;
+    for (int i = 0; i < B->count; i++) {
+      off[i] = tot;
+      tot += seq_scratch_doubles(B->n[i], B->nsteps[i]);
+    }
+    int rc;
+    if ((rc = dalloc(&B->d_seq, (size_t)tot)) || (rc = dalloc(&B->d_seq_off, (size_t)B->count))) return rc;
+    CK(cudaMemcpyAsync(B->d_seq_off, off.data(), B->count * sizeof(long long), cudaMemcpyHostToDevice, B->st));
+  }
+  CK(seq_propagate_launch(batch_dev(B), scheme, wmode, B->d_seq, B->d_seq_off, B->st));
+  g_launches++;
+  return SCFT_OK;
+}
+
 // Reset the per-instance solver state on B->st and describe it to the mixing step.
 static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool verify, MixDev *mp) {
   cudaStream_t st = B->st;
@@ -704,9 +743,10 @@ static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res
     const int li = live_index(B, 0, p, (int)i);
     d.work = B->d_work + li;
     // keep the class's share resident if the fused kernel fits fewer CTAs per SM
-    int grid = c.grid, occ = 0;
-    CK(solve_dispatch(c.C, c.NW, b, d, m, 0, s, &occ));
-    const int pocc = propagate_ctas_per_sm(p, c.C, c.NW);
+    // than the plan assumed
+    int grid = c.grid;
+    const int occ = solve_ctas_per_sm(c.C, c.NW);
+    const int pocc = std::max(propagate_ctas_per_sm(p, c.C, c.NW), occ);
     if (occ <= 0) return set_err(SCFT_ECUDA, "fused solve of class (%d, %d) does not fit an SM", c.C, c.NW);
     if (pocc > occ) grid = std::max(1, (int)((long long)c.grid * occ / pocc));
     d.workers = std::min(c.workers, grid * c.gpc);
@@ -902,7 +942,7 @@ static int autotune(scft_batch *B, int p) {
 // ---------------------------------------------------------------------------
 struct DropIn {
   bool set = false;
-  int n = 0, nsteps = 0, rule = 0, sign = 1, prec = PREC_F64;
+  int n = 0, nsteps = 0, rule = 0, sign = 1, prec = PREC_F64, scheme = SCFT_SCHEME_IE, wmode = SCFT_W_ROWSCALED;
   double ds = 0, L = 0;
   std::vector<double> x, f0;
   scft_batch *B = nullptr;
@@ -921,7 +961,9 @@ static int dropin_eval_device(const double *d_xint, double *d_out, int fixed_poi
   CK(cudaMemcpyAsync(B->d_w + 1, d_xint, N * sizeof(double), cudaMemcpyDeviceToDevice, B->st));
   int rc = fill_int(B->d_active, 1, D.prec == PREC_F32 ? 1 : 2, B->st);
   if (rc) return rc;
-  if ((rc = enqueue_propagate(B, D.prec))) return rc;
+  if (D.scheme != SCFT_SCHEME_IE || D.wmode != SCFT_W_ROWSCALED) rc = seq_enqueue(B, D.scheme, D.wmode);
+  else rc = enqueue_propagate(B, D.prec);
+  if (rc) return rc;
   CK(residual_launch(D.n, B->d_phi, B->d_f0, D.sign, d_out, B->d_w + 1, fixed_point, B->st));
   g_launches++;
   return SCFT_OK;
@@ -1272,8 +1314,12 @@ void scft_config_init(scft_config *c) {
 int scft_set_config(const scft_config *c) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   if (!c || c->n_nodes < 3 || !c->f0 || c->nsteps < 1 || !(c->ds > 0.0) ||
-      (c->precision != SCFT_F32 && c->precision != SCFT_F64))
+      (c->precision != SCFT_F32 && c->precision != SCFT_F64) ||
+      (c->scheme != SCFT_SCHEME_IE && c->scheme != SCFT_SCHEME_IRK2) ||
+      (c->wmode != SCFT_W_ROWSCALED && c->wmode != SCFT_W_CONSISTENT))
     return set_err(SCFT_EINVAL, "scft_set_config: invalid configuration");
+  if ((c->scheme != SCFT_SCHEME_IE || c->wmode != SCFT_W_ROWSCALED) && c->precision != SCFT_F64)
+    return set_err(SCFT_EINVAL, "scft_set_config: the IRK2 scheme and the consistent field term run in FP64");
   DropIn &D = g_drop;
   if (D.B) { destroy_batch(D.B); D.B = nullptr; }
   dfree(D.d_in); dfree(D.d_out);
@@ -1282,6 +1328,7 @@ int scft_set_config(const scft_config *c) {
   D.set = false;
   D.n = c->n_nodes; D.nsteps = c->nsteps; D.ds = c->ds; D.rule = c->rule;
   D.sign = c->sign >= 0 ? 1 : -1; D.prec = c->precision;
+  D.scheme = c->scheme; D.wmode = c->wmode;
   D.x.resize(D.n);
   D.f0.assign(c->f0, c->f0 + D.n);
   D.L = c->x ? c->x[D.n - 1] - c->x[0] : c->L;
@@ -1290,6 +1337,10 @@ int scft_set_config(const scft_config *c) {
   scft_instance inst;
   inst.n_nodes = D.n; inst.x = D.x.data(); inst.L = D.L; inst.f0 = D.f0.data(); inst.w0 = nullptr;
   inst.nsteps = D.nsteps; inst.ds = D.ds; inst.rule = D.rule;
+  std::vector<double> w0(D.n, 0.0);
+  w0[0] = c->w_wall[0];
+  w0[D.n - 1] = c->w_wall[1];
+  inst.w0 = w0.data();  // interior values come with every evaluation; wall values stay
   int rc = create_batch(&inst, 1, &D.B);
   if (rc) return rc;
   if ((rc = plan(D.B, D.prec, 1.0))) return rc;
@@ -1329,9 +1380,11 @@ int scft_density(const double *w_nodes, double *phi, double *Q) {
   if (!D.set) return set_err(SCFT_ENOCONFIG, "scft_set_config was not called");
   if (!w_nodes || !phi) return set_err(SCFT_EINVAL, "scft_density: null buffer");
   std::vector<double> w(w_nodes, w_nodes + D.n);
-  w[0] = w[D.n - 1] = 0.0;
+  if (D.wmode == SCFT_W_ROWSCALED) w[0] = w[D.n - 1] = 0.0;  // the consistent term uses the wall values
   CK(cudaMemcpy(D.B->d_w, w.data(), D.n * sizeof(double), cudaMemcpyHostToDevice));
-  int rc = evaluate(D.B, D.prec);
+  int rc = (D.scheme != SCFT_SCHEME_IE || D.wmode != SCFT_W_ROWSCALED)
+               ? scft_batch_evaluate_scheme(D.B, D.scheme, D.wmode)
+               : evaluate(D.B, D.prec);
   if (rc) return rc;
   CK(cudaMemcpy(phi, D.B->d_phi, D.n * sizeof(double), cudaMemcpyDeviceToHost));
   if (Q) CK(cudaMemcpy(Q, D.B->d_Q, sizeof(double), cudaMemcpyDeviceToHost));
@@ -1501,6 +1554,19 @@ int scft_batch_set_fields(scft_batch *b, const double *w_nodes) {
 int scft_batch_evaluate(scft_batch *b, int precision) {
   if (!b) return set_err(SCFT_EINVAL, "scft_batch_evaluate");
   return evaluate(b, precision);
+}
+
+int scft_batch_evaluate_scheme(scft_batch *b, int scheme, int wmode) {
+  if (!b) return set_err(SCFT_EINVAL, "scft_batch_evaluate_scheme");
+  int rc = fill_int(b->d_active, b->count, 2, b->st);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(b->d_status, 0, b->count * sizeof(int), b->st));
+  CK(cudaEventRecord(b->t0, b->st));
+  if ((rc = seq_enqueue(b, scheme, wmode))) return rc;
+  CK(cudaEventRecord(b->t1, b->st));
+  CK(cudaStreamSynchronize(b->st));
+  CK(cudaEventElapsedTime(&b->last_ms, b->t0, b->t1));
+  return SCFT_OK;
 }
 
 int scft_batch_solve(scft_batch *b, const scft_solve_opts *opts, scft_result *res) {

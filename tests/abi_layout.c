@@ -11,7 +11,7 @@ int main(void) {
   printf("scft_config %zu\n", sizeof(scft_config));
   F(scft_config, n_nodes); F(scft_config, x); F(scft_config, L); F(scft_config, f0);
   F(scft_config, nsteps); F(scft_config, ds); F(scft_config, rule); F(scft_config, sign);
-  F(scft_config, precision);
+  F(scft_config, precision); F(scft_config, scheme); F(scft_config, wmode); F(scft_config, w_wall);
   printf("scft_instance %zu\n", sizeof(scft_instance));
   F(scft_instance, n_nodes); F(scft_instance, x); F(scft_instance, L); F(scft_instance, f0);
   F(scft_instance, w0); F(scft_instance, nsteps); F(scft_instance, ds); F(scft_instance, rule);
