@@ -180,12 +180,12 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic(workload: str, C: int, NW: int, alg_bytes: float):
+def committed_traffic(workload: str, C: int, NW: int, alg_bytes: float, fused: bool):
     """DRAM bytes per launch of the dominant kernel: the committed ncu summary
     of this workload gives, per shape class, DRAM bytes (read + write) per
     algorithmic byte measured on a smaller launch of the same class; scaled to
     this launch by its algorithmic bytes."""
-    path = os.path.join(ROOT, "profiles", f"propagate_f32_{workload}.md")
+    path = os.path.join(ROOT, "profiles", f"{'solve' if fused else 'propagate'}_f32_{workload}.md")
     if not os.path.exists(path):
         return None
     key = f"dram_traffic_per_algorithmic_byte <float,{C},{NW}>:"
@@ -325,12 +325,13 @@ def ours_arm(args):
     (dC, dNW), (dl, dby, dms) = max(live.items(), key=lambda kv: kv[1][2])
     peak, peak_kind = peaks()
     achieved = dby / (dms / 1e3) / 1e9
-    traffic = committed_traffic(args.workload, dC, dNW, dby / dl)
+    traffic = committed_traffic(args.workload, dC, dNW, dby / dl, bool(opts.fused))
     # the same classes, one full pass each with the class alone on the GPU
     prof = b.profile(F32)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_kind,
-                "kernel": f"propagate_kernel<float,C={dC},NW={dNW},increment form>",
+                "kernel": (f"solve_kernel<float,C={dC},NW={dNW}> (fused contour passes and Anderson steps)"
+                           if opts.fused else f"propagate_kernel<float,C={dC},NW={dNW},increment form>"),
                 "launches": dl, "bytes_per_launch": dby / dl, "ms_per_launch": dms / dl,
                 "live_classes": [{"C": k[0], "NW": k[1], "launches": v[0], "bytes": v[1], "ms": v[2],
                                   "GBps": v[1] / (v[2] / 1e3) / 1e9 if v[2] > 0 else None}
@@ -537,6 +538,28 @@ def config_legs(ws):
     return out
 
 
+def profile_solve(args):
+    """One fused FP32 solve of the workload (learned warm start) after one
+    warm-up solve: the small, self-contained command the ncu capture of the
+    fused solve kernel runs."""
+    import torch
+
+    from scft_gb300 import F32, api
+    from scft_gb300.warmstart import WarmStart
+
+    insts, _ = make_workload(args.workload, args.count)
+    ws = WarmStart(bf16=True)
+    ws.load(args.weights)
+    with api.Batch(insts) as b:
+        for _ in range(2):
+            ws.predict(b)
+            r = b.solve(api.solve_opts(precision=F32, tol=TOL))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_solve": args.workload, "instances": len(insts), "ms": b.last_ms(),
+                          "iterations_mean": float(r["iterations"].mean()), "live": b.live_stats(F32)}))
+    return 0
+
+
 def profile_pass(args):
     """One FP32 propagator pass over the workload after one warm-up pass: the
     small, self-contained command the ncu captures run."""
@@ -572,9 +595,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workload configs")
     ap.add_argument("--profile-pass", action="store_true", help="one FP32 propagator pass (for ncu)")
+    ap.add_argument("--profile-solve", action="store_true", help="one fused FP32 solve (for ncu)")
     args = ap.parse_args()
     if args.profile_pass:
         return profile_pass(args)
+    if args.profile_solve:
+        return profile_solve(args)
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     return reference_arm(args) if args.impl == "reference" else ours_arm(args)
