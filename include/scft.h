@@ -188,6 +188,14 @@ int scft_batch_set_fields(scft_batch *b, const double *w_nodes);
 int scft_batch_evaluate(scft_batch *b, int precision);
 /* Solve every instance to opts->tol; res (count entries) may be NULL. */
 int scft_batch_solve(scft_batch *b, const scft_solve_opts *opts, scft_result *res);
+/* Enqueues the fused FP32 solve of b (opts as scft_batch_solve; fused = 1,
+   verify64 = 0) on b's own streams and returns without waiting; scft_batch_wait
+   completes it (results as scft_batch_solve).  Solves of different batches in
+   flight at the same time share the GPU: while one batch's slowest instances run
+   their last iterations, the next batch's instances take the SMs that have
+   emptied.  One solve per batch may be in flight. */
+int scft_batch_solve_async(scft_batch *b, const scft_solve_opts *opts);
+int scft_batch_wait(scft_batch *b, scft_result *res);
 /* Copy fields / densities (concatenated n_nodes per instance) and Q out; any may be NULL. */
 int scft_batch_get(scft_batch *b, double *w_nodes, double *phi_nodes, double *Q);
 /* Restore every field to the w0 given at creation (device copy, no host traffic). */

@@ -101,6 +101,8 @@ SIGNATURES = {
     "scft_batch_destroy": (C.c_int, [C.c_void_p]),
     "scft_kernel_launches": (C.c_longlong, []),
     "scft_mem_trim": (C.c_longlong, []),
+    "scft_batch_solve_async": (C.c_int, [C.c_void_p, C.POINTER(ScftSolveOpts)]),
+    "scft_batch_wait": (C.c_int, [C.c_void_p, C.POINTER(ScftResult)]),
     "scft_batch_evaluate_scheme": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "scft_ws_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "scft_ws_destroy": (C.c_int, [C.c_void_p]),

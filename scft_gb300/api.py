@@ -315,6 +315,22 @@ class Batch:
             "Q": np.array([r.Q for r in res]),
         }
 
+    def solve_async(self, opts: L.ScftSolveOpts | None = None, **kw):
+        """Enqueue the fused FP32 solve and return at once; wait() completes it.
+        Batches solving at the same time share the GPU."""
+        o = opts if opts is not None else solve_opts(**kw)
+        check(self.lib.scft_batch_solve_async(self.h, C.byref(o)), "scft_batch_solve_async")
+
+    def wait(self):
+        res = (L.ScftResult * self.count)()
+        check(self.lib.scft_batch_wait(self.h, res), "scft_batch_wait")
+        return {
+            "status": np.array([r.status for r in res]),
+            "iterations": np.array([r.iterations for r in res]),
+            "err": np.array([r.err for r in res]),
+            "Q": np.array([r.Q for r in res]),
+        }
+
     def get(self):
         tot = int(self.offsets[-1])
         w = np.empty(tot)

@@ -1,9 +1,11 @@
 // batch.cuh -- internal layout of a batch (shared by the runtime and the
 // warm-start network; not part of the C ABI).
 #pragma once
+#include <chrono>
 #include <vector>
 
 #include "common.cuh"
+#include "mixing.cuh"
 #include "scft.h"
 
 struct ClassPlan {
@@ -59,6 +61,11 @@ struct scft_batch {
   int live_cap = 0, live_maxc = 0;
   std::vector<double> live_ms[2], live_units[2];
   std::vector<long long> live_launches[2];
+  // a fused solve enqueued by scft_batch_solve_async, completed by scft_batch_wait
+  bool pending = false;
+  scft_solve_opts pending_opts{};
+  scft::MixDev pending_mix{};
+  std::chrono::steady_clock::time_point pending_start{};
 };
 
 

@@ -719,20 +719,21 @@ static int graph_iterate(scft_batch *B, const scft_solve_opts *o, const MixDev &
 // (most expensive first) and iterates each one to the end on its own, the
 // contour pass and the Anderson step back to back, so no instance waits for a
 // batch-wide iteration.  Every loop is bounded by the iteration limit.
-static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
   const int p = PREC_F32;
   int rc;
   if ((rc = live_prepare(B, 1))) return rc;
   cudaStream_t st = B->st;
   auto &plans = B->plans[p];
   CK(cudaEventRecord(B->t0, st));
-  MixDev m;
+  MixDev &m = B->pending_mix;
   if ((rc = solve_begin(B, o, p, false, &m))) return rc;
+  B->pending_opts = *o;
   const size_t live_bytes = (size_t)2 * B->live_maxc * sizeof(unsigned long long);
   CK(cudaMemsetAsync(B->d_work, 0, live_bytes, st));
   for (auto &c : plans) CK(cudaMemsetAsync(B->d_heads + c.head, 0, sizeof(int), st));
   const BatchDev b = batch_dev(B);
-  const auto t_start = std::chrono::steady_clock::now();
+  B->pending_start = std::chrono::steady_clock::now();
   CK(cudaEventRecord(B->ev_fork, st));
   for (size_t i = 0; i < plans.size(); i++) {
     const ClassPlan &c = plans[i];
@@ -758,23 +759,34 @@ static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res
   }
   for (size_t i = 0; i < plans.size(); i++) CK(cudaStreamWaitEvent(st, B->ev_join[i], 0));
   CK(cudaMemcpyAsync(B->h_work, B->d_work, live_bytes, cudaMemcpyDeviceToHost, st));
-  CK(cudaEventRecord(B->t1, st));
-  cudaError_t e = cudaEventSynchronize(B->t1);
-  if (e != cudaSuccess) return set_err(SCFT_ECUDA, "fused solve: %s", cudaGetErrorString(e));
-  if ((rc = live_collect(B, 1, true, false))) return rc;
-  // instances whose FP32 iteration stalled (active == 2) finish with the FP64
-  // propagator, batch-wide iterations over those instances only
   count_active_kernel<<<1, 256, 0, st>>>(B->d_active, B->count, B->d_nactive);
   g_launches++;
   CK(cudaMemcpyAsync(B->h_nactive, B->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+  CK(cudaEventRecord(B->t1, st));
+  B->pending = true;
+  return SCFT_OK;
+}
+
+// Completes the solve enqueued by solve_fused_enqueue: statistics, the FP64
+// continuation of instances whose FP32 iteration stalled, results.
+static int solve_fused_finish(scft_batch *B, scft_result *res) {
+  if (!B->pending) return set_err(SCFT_EINVAL, "no solve of this batch is in flight");
+  B->pending = false;
+  cudaStream_t st = B->st;
+  int rc;
+  cudaError_t e = cudaEventSynchronize(B->t1);
+  if (e != cudaSuccess) return set_err(SCFT_ECUDA, "fused solve: %s", cudaGetErrorString(e));
+  if ((rc = live_collect(B, 1, true, false))) return rc;
   B->trace_active.assign(1, *B->h_nactive);
-  B->trace_ms.assign(1, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
+  B->trace_ms.assign(1, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
+                                                                   B->pending_start).count());
+  // instances whose FP32 iteration stalled (active == 2) finish with the FP64
+  // propagator, batch-wide iterations over those instances only
   if (*B->h_nactive > 0) {
     if ((rc = plan(B, PREC_F64, 1.0))) return rc;
     std::vector<double> ms32 = B->live_ms[PREC_F32], un32 = B->live_units[PREC_F32];
     std::vector<long long> ln32 = B->live_launches[PREC_F32];
-    if ((rc = graph_iterate(B, o, m, false, true))) return rc;
+    if ((rc = graph_iterate(B, &B->pending_opts, B->pending_mix, false, true))) return rc;
     // keep the fused launch's statistics for the FP32 classes
     B->live_ms[PREC_F32] = ms32; B->live_units[PREC_F32] = un32; B->live_launches[PREC_F32] = ln32;
     CK(cudaEventRecord(B->t1, st));
@@ -782,6 +794,12 @@ static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res
   }
   CK(cudaEventElapsedTime(&B->last_ms, B->t0, B->t1));
   return solve_results(B, res);
+}
+
+static int solve_fused(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+  int rc = solve_fused_enqueue(B, o);
+  if (rc) return rc;
+  return solve_fused_finish(B, res);
 }
 
 // Batch-wide iterations replayed from a CUDA graph until no instance is active:
@@ -855,11 +873,18 @@ static int graph_iterate(scft_batch *B, const scft_solve_opts *o, const MixDev &
   return result;
 }
 
-static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+static int check_opts(const scft_solve_opts *o) {
   const int p = o->precision;
   if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
       !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0)
     return set_err(SCFT_EINVAL, "solve options");
+  return SCFT_OK;
+}
+
+static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+  const int p = o->precision;
+  if (check_opts(o)) return SCFT_EINVAL;
+  if (B->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
   int rc = plan(B, p, 1.0);
   if (rc) return rc;
   const bool verify = (p == PREC_F32) && o->verify64;
@@ -1574,6 +1599,25 @@ int scft_batch_solve(scft_batch *b, const scft_solve_opts *opts, scft_result *re
   scft_solve_opts o;
   scft_solve_opts_init(&o);
   return solve(b, opts ? opts : &o, res);
+}
+
+int scft_batch_solve_async(scft_batch *b, const scft_solve_opts *opts) {
+  if (!b) return set_err(SCFT_EINVAL, "scft_batch_solve_async");
+  scft_solve_opts d;
+  scft_solve_opts_init(&d);
+  const scft_solve_opts *o = opts ? opts : &d;
+  if (check_opts(o)) return SCFT_EINVAL;
+  if (o->precision != PREC_F32 || !o->fused || o->verify64)
+    return set_err(SCFT_EINVAL, "asynchronous solves run the fused FP32 form (fused = 1, verify64 = 0)");
+  if (b->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
+  int rc;
+  if ((rc = plan(b, PREC_F32, 1.0)) || (rc = ensure_mix(b, o->depth))) return rc;
+  return solve_fused_enqueue(b, o);
+}
+
+int scft_batch_wait(scft_batch *b, scft_result *res) {
+  if (!b) return set_err(SCFT_EINVAL, "scft_batch_wait");
+  return solve_fused_finish(b, res);
 }
 
 int scft_batch_get(scft_batch *b, double *w_nodes, double *phi_nodes, double *Q) {

@@ -256,3 +256,27 @@ def test_released_memory_is_reused_and_trimmed(lib):
         np.testing.assert_array_equal(a, c)
     assert lib.scft_mem_trim() > 0
     assert lib.scft_mem_trim() == 0
+
+
+def test_async_solves_in_flight_together_match_the_synchronous_solve():
+    """Two batches solved asynchronously at the same time share the GPU; every
+    instance iterates exactly as in a synchronous solve (bit-identical fields)."""
+    ia, ib = W.batch_mixed(48, seed=91), W.batch_mixed(40, seed=92)
+    with api.Batch(ia) as A, api.Batch(ib) as B:
+        ra, rb = A.solve(), B.solve()
+        wa, wb = A.get()[0], B.get()[0]
+        A.reset()
+        B.reset()
+        A.solve_async(api.solve_opts())
+        B.solve_async(api.solve_opts())
+        with pytest.raises(Exception):
+            A.solve_async(api.solve_opts())  # one solve per batch in flight
+        ra2, rb2 = A.wait(), B.wait()
+        with pytest.raises(Exception):
+            A.wait()  # nothing in flight any more
+        np.testing.assert_array_equal(ra2["iterations"], ra["iterations"])
+        np.testing.assert_array_equal(rb2["iterations"], rb["iterations"])
+        for x, y in zip(A.get()[0], wa):
+            np.testing.assert_array_equal(x, y)
+        for x, y in zip(B.get()[0], wb):
+            np.testing.assert_array_equal(x, y)
