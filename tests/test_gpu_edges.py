@@ -1,0 +1,65 @@
+"""Edge cases of the batched path through the C ABI: the largest instance the
+propagator shapes cover (32 warps x 32 lanes x 8 unknowns = 8192 interior
+nodes) against the oracle, one node more rejected, empty and malformed batches
+rejected with SCFT_EINVAL, a one-element mesh edge (one interior node), and
+instances that differ only in their contour step counts (odd, even, powers of
+two and not) in one batch."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from scft_gb300 import F32, F64, RULE_ROMBERG, RULE_TRAPEZOID, ScftError, _lib, api, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_largest_instance_matches_oracle_and_one_more_node_is_rejected(oracle):
+    d = W.instance(8193, 12.0, 64, 3, 0)   # 8194 nodes: 8192 interior unknowns
+    assert d["n_nodes"] - 2 == 32 * 32 * 8
+    p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"])
+    phi_ref, q_ref = oracle.propagate(p, d["w0"])
+    with api.Batch([d]) as b:
+        for prec, tol in ((F64, 1e-10), (F32, 1e-5)):
+            b.evaluate(prec)
+            _, phi, Q = b.get()
+            assert rel(phi[0], phi_ref) <= tol, (prec, rel(phi[0], phi_ref))
+            assert abs(Q[0] - q_ref) <= tol * abs(q_ref)
+    big = W.instance(8194, 12.0, 64, 3, 0)
+    with api.Batch([big]) as b:
+        with pytest.raises(ScftError) as e:
+            b.evaluate(F32)
+        assert e.value.code == _lib.SCFT_EINVAL
+
+
+def test_empty_and_malformed_batches_are_rejected():
+    with pytest.raises(ScftError) as e:
+        api.Batch([])
+    assert e.value.code == _lib.SCFT_EINVAL
+    good = W.instance(16, 4.0, 64, 1, 0)
+    bad = [dict(good, nsteps=0), dict(good, ds=-1.0), dict(good, rule=7),
+           dict(good, x=good["x"][::-1].copy()), dict(good, nsteps=48, rule=RULE_ROMBERG)]
+    for d in bad:
+        with pytest.raises(ScftError) as e:
+            api.Batch([good, d])
+        assert e.value.code == _lib.SCFT_EINVAL
+
+
+def test_single_interior_node_and_ragged_step_counts(oracle):
+    insts = [W.instance(2, 3.0, 16, 4, 0),                                # one interior node
+             W.instance(40, 5.0, 777, 4, 1, rule=RULE_TRAPEZOID),        # odd step count
+             W.instance(40, 5.0, 1000, 4, 2, rule=RULE_TRAPEZOID),       # even, not a power of two
+             W.instance(40, 5.0, 4096, 4, 3),
+             W.instance(41, 5.0, 16, 4, 4)]
+    with api.Batch(insts) as b:
+        for prec, tol in ((F64, 1e-10), (F32, 1e-5)):
+            b.evaluate(prec)
+            _, phi, Q = b.get()
+            for i, d in enumerate(insts):
+                p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d["rule"])
+                phi_ref, q_ref = oracle.propagate(p, d["w0"])
+                assert rel(phi[i], phi_ref) <= tol, (prec, i, rel(phi[i], phi_ref))
+                assert abs(Q[i] - q_ref) <= tol * abs(q_ref), (prec, i)
