@@ -166,6 +166,9 @@ typedef struct scft_solve_opts {
                          history, tolerance tol, status bit SCFT_ST_FP64); 0: off.  FP32 rounding
                          noise in the density (~1e-7) corrupts the secant pairs of small steps */
   double finish_tol;
+  double budget_ms;   /* > 0: device-side time budget of the solve; a thread group that finds it
+                         spent at an iteration boundary stops its instance with SCFT_ST_WATCHDOG
+                         (the solve returns normally); 0: none */
 } scft_solve_opts;
 
 typedef struct scft_result {

@@ -57,7 +57,7 @@ class ScftSolveOpts(C.Structure):
                 ("residual_mode", C.c_int), ("precond", C.c_double), ("iters_per_graph", C.c_int),
                 ("beta_schedule", C.c_int), ("weighted", C.c_int), ("step_cap", C.c_double),
                 ("field_floor", C.c_double), ("fused", C.c_int),
-                ("finish_stall", C.c_int), ("finish_tol", C.c_double)]
+                ("finish_stall", C.c_int), ("finish_tol", C.c_double), ("budget_ms", C.c_double)]
 
 
 class ScftResult(C.Structure):

@@ -45,6 +45,7 @@ struct scft_batch {
   double *d_seq = nullptr;
   long long *d_seq_off = nullptr;
   int *d_ref_it = nullptr;
+  unsigned long long *d_deadline = nullptr;
   int *d_iters = nullptr, *d_hcount = nullptr, *d_hhead = nullptr, *d_nactive = nullptr;
   int *h_nactive = nullptr;
   std::vector<int> trace_active;   // unfinished instances after each graph launch of the last solve

@@ -54,6 +54,12 @@ __device__ inline void small_solve(double *A, double *b, int k) {
 }
 
 // Shared memory of one group's mixing step.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 template <int NW>
 struct MixSmem {
   double sm[NW];
@@ -61,6 +67,7 @@ struct MixSmem {
   double gam[MIX_MAXD];
   int slot[MIX_MAXD];
   int ctl[4];
+  int stop;
 };
 
 // Group-wide max of v (every thread of the group receives it).
@@ -129,6 +136,15 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
   if (it >= m.maxit) {
     if (tid == 0) { m.status[inst] |= ST_MAXIT; m.active[inst] = 0; m.err[inst] = e; }
     return true;
+  }
+  // time budget: one thread reads the clock, the whole group follows its decision
+  if (m.deadline) {
+    if (tid == 0) S.stop = global_ns() > __ldcg(m.deadline) ? 1 : 0;
+    sync();
+    if (S.stop) {
+      if (tid == 0) { m.status[inst] |= ST_WATCHDOG; m.active[inst] = 0; m.err[inst] = e; }
+      return true;
+    }
   }
   // FP32 stall: below finish_tol and no halving of the error for finish_stall
   // iterations -> the FP64 propagator continues from this field with a fresh

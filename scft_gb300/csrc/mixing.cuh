@@ -41,6 +41,9 @@ struct MixDev {
   double finish_tol;
   double *ref_err;
   int *ref_it;
+  // time budget: globaltimer (ns) after which a group stops its instance with
+  // ST_WATCHDOG at the next iteration boundary; null: no budget
+  const unsigned long long *deadline;
 };
 
 cudaError_t mix_launch(const MixDev &m, cudaStream_t st);

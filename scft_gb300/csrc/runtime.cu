@@ -434,6 +434,13 @@ __global__ void fill_double_kernel(double *a, long long n, double v) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) a[i] = v;
 }
+// The solve's deadline on the device clock: now + budget.
+__global__ void set_deadline_kernel(unsigned long long *deadline, unsigned long long budget_ns) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  *deadline = t + budget_ns;
+}
+
 __global__ void count_active_kernel(const int *a, int n, int *out) {
   __shared__ int s;
   if (threadIdx.x == 0) s = 0;
@@ -463,7 +470,7 @@ static int fill_double(double *a, long long n, double v, cudaStream_t st) {
 static void free_mix(scft_batch *B) {
   dfree(B->d_graw); dfree(B->d_gcur); dfree(B->d_gprev); dfree(B->d_wprev);
   dfree(B->d_hdx); dfree(B->d_hdg); dfree(B->d_gram); dfree(B->d_err); dfree(B->d_best); dfree(B->d_lk);
-  dfree(B->d_ref_err); dfree(B->d_ref_it);
+  dfree(B->d_ref_err); dfree(B->d_ref_it); dfree(B->d_deadline);
   dfree(B->d_iters); dfree(B->d_hcount); dfree(B->d_hhead); dfree(B->d_nactive);
   if (B->h_nactive) host_free(B->h_nactive);
   B->h_nactive = nullptr;
@@ -480,7 +487,7 @@ static int ensure_mix(scft_batch *B, int depth) {
       (rc = dalloc(&B->d_hdg, ni * depth)) || (rc = dalloc(&B->d_gram, c * depth * depth)) ||
       (rc = dalloc(&B->d_err, c)) || (rc = dalloc(&B->d_best, c)) || (rc = dalloc(&B->d_lk, c)) || (rc = dalloc(&B->d_iters, c)) ||
       (rc = dalloc(&B->d_hcount, c)) || (rc = dalloc(&B->d_hhead, c)) || (rc = dalloc(&B->d_nactive, 1)) ||
-      (rc = dalloc(&B->d_ref_err, c)) || (rc = dalloc(&B->d_ref_it, c)))
+      (rc = dalloc(&B->d_ref_err, c)) || (rc = dalloc(&B->d_ref_it, c)) || (rc = dalloc(&B->d_deadline, 1)))
     return rc;
   CK(host_alloc((void **)&B->h_nactive, sizeof(int)));
   B->depth = depth;
@@ -695,6 +702,13 @@ static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool veri
   m.finish_stall = (p == PREC_F32) ? o->finish_stall : 0;
   m.finish_tol = o->finish_tol;
   m.ref_err = B->d_ref_err; m.ref_it = B->d_ref_it;
+  m.deadline = nullptr;
+  if (o->budget_ms > 0.0) {
+    set_deadline_kernel<<<1, 1, 0, st>>>(B->d_deadline, (unsigned long long)(o->budget_ms * 1e6));
+    g_launches++;
+    CK(cudaGetLastError());
+    m.deadline = B->d_deadline;
+  }
   return SCFT_OK;
 }
 
@@ -876,7 +890,7 @@ static int graph_iterate(scft_batch *B, const scft_solve_opts *o, const MixDev &
 static int check_opts(const scft_solve_opts *o) {
   const int p = o->precision;
   if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
-      !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0)
+      !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0 || !(o->budget_ms >= 0.0))
     return set_err(SCFT_EINVAL, "solve options");
   return SCFT_OK;
 }
@@ -1544,6 +1558,7 @@ int scft_broydn(double *x, int n, int *check, scft_vecfunc f) {
 
 void scft_solve_opts_init(scft_solve_opts *o) {
   if (!o) return;
+  memset(o, 0, sizeof *o);
   o->precision = SCFT_F32;
   o->tol = 1e-6;
   o->tol32_factor = 0.5;
@@ -1564,6 +1579,7 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->fused = 1;
   o->finish_stall = 0;
   o->finish_tol = 1e-4;
+  o->budget_ms = 0.0;
 }
 
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {

@@ -22,7 +22,7 @@ int main(void) {
   F(scft_solve_opts, residual_mode); F(scft_solve_opts, precond); F(scft_solve_opts, iters_per_graph);
   F(scft_solve_opts, beta_schedule); F(scft_solve_opts, weighted); F(scft_solve_opts, step_cap);
   F(scft_solve_opts, field_floor); F(scft_solve_opts, fused);
-  F(scft_solve_opts, finish_stall); F(scft_solve_opts, finish_tol);
+  F(scft_solve_opts, finish_stall); F(scft_solve_opts, finish_tol); F(scft_solve_opts, budget_ms);
   printf("scft_result %zu\n", sizeof(scft_result));
   F(scft_result, status); F(scft_result, iterations); F(scft_result, err); F(scft_result, Q);
   return 0;

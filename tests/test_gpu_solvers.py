@@ -280,3 +280,34 @@ def test_async_solves_in_flight_together_match_the_synchronous_solve():
             np.testing.assert_array_equal(x, y)
         for x, y in zip(B.get()[0], wb):
             np.testing.assert_array_equal(x, y)
+
+
+def test_spent_time_budget_stops_every_instance_with_watchdog_status():
+    """A device-side budget far below one contour pass: every group stops its
+    instance at its first iteration boundary with the watchdog bit, in both solve
+    forms, and the solve returns normally."""
+    insts = W.batch_mixed(32, seed=93)
+    with api.Batch(insts) as b:
+        for fused in (1, 0):
+            b.reset()
+            r = b.solve(api.solve_opts(precision=F32, tol=1e-6, budget_ms=1e-6, fused=fused))
+            assert np.all(r["status"] & 32), (fused, r["status"])
+            assert not np.any(r["status"] & ST_CONVERGED)
+            assert r["iterations"].max() <= 1
+        b.reset()
+        r = b.solve(api.solve_opts(precision=F32, tol=1e-6, budget_ms=60000.0))
+        assert np.all(r["status"] & ST_CONVERGED) and not np.any(r["status"] & 32)
+
+
+def test_non_finite_field_is_flagged_and_the_rest_converge():
+    """A NaN field in one instance: that instance stops with the non-finite bit,
+    every other instance of the batch converges."""
+    insts = W.batch_mixed(16, seed=94)
+    with api.Batch(insts) as b:
+        w = [d["w0"].copy() for d in insts]
+        w[5][len(w[5]) // 2] = np.nan
+        b.set_fields(w)
+        r = b.solve(api.solve_opts(precision=F32, tol=1e-6))
+        assert r["status"][5] & 2 and not r["status"][5] & ST_CONVERGED
+        others = np.delete(r["status"], 5)
+        assert np.all(others & ST_CONVERGED)
