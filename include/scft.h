@@ -335,6 +335,24 @@ int scft_field_write(const char *path, int n_nodes, const double *x, const doubl
    |f|max (NAN when absent; may be NULL). */
 int scft_res_read(const char *path, int max_rows, int *rows, double *table, int *m, int *nsteps, double *header);
 
+/* =========================================================================
+ * Mesh refinement and field transfer of the deal.II driver (refine_mesh,
+ * DEALII_SCFT/src/scft.cc:132-166).
+ * ========================================================================= */
+
+/* Bisects every element of the mesh x (n_nodes points) into x_new (2 n_nodes - 1
+   points), the refinement refine_mesh applies (every cell is cut in x). */
+int scft_refine_bisect(int n_nodes, const double *x, double *x_new);
+/* Cubic splines of `count` tables, evaluated on the GPU (FP64): table t has
+   nx[t] points (x, y; concatenated over the tables, x strictly increasing) and
+   is evaluated at nxp[t] points (xp, concatenated) into yp.  The spline of
+   spline_chen (spline_chen.c:13-106): m == NULL gives not-a-knot ends (nx >= 4),
+   otherwise the second derivative *m at both ends; points outside a table take
+   its end cubic.  refine_mesh transfers the interior field with
+   spline_chen(&x[1], &w[1], &x_new[1], &w_new[1], n - 2, n_new - 2, NULL). */
+int scft_spline(int count, const int *nx, const double *x, const double *y, const int *nxp, const double *xp,
+                double *yp, const double *m);
+
 /* The library keeps the device and pinned host blocks it releases (batches,
    scratch, warm-start buffers) for reuse, so creating a batch per request does
    not call cudaMalloc/cudaFree again; a failed allocation releases the cache and

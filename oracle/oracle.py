@@ -115,6 +115,7 @@ class Oracle:
         L.or_mesh_uniform.argtypes = [C.c_int, C.c_double, _dp]
         L.or_f0_tanh2_ceil.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
         L.or_f0_tanh2_le.argtypes = [C.c_int, _dp, C.c_double, _dp]
+        L.or_spline.argtypes = [_dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp]
         L.or_f0_gauss_wall.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
         L.or_anderson_solve.argtypes = [C.POINTER(Problem), _dp, C.POINTER(MixOpts),
                                         C.POINTER(C.c_int), C.POINTER(C.c_double)]
@@ -136,6 +137,14 @@ class Oracle:
         f = np.empty(len(x)); x = np.ascontiguousarray(x, dtype=np.float64)
         self.L.or_f0_tanh2_ceil(len(x), _ptr(x), tau, L, _ptr(f))
         return f
+
+    def spline(self, x, y, xp, m=None):
+        """spline_chen.c:13-106 restated: (rc, yp)."""
+        x, y, xp = (np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, xp))
+        yp = np.empty(len(xp))
+        mm = None if m is None else np.array([m], dtype=np.float64)
+        rc = self.L.or_spline(_ptr(x), _ptr(y), len(x), _ptr(xp), _ptr(yp), len(xp), None if mm is None else _ptr(mm))
+        return rc, yp
 
     def f0_tanh2_le(self, x, tau):
         f = np.empty(len(x)); x = np.ascontiguousarray(x, dtype=np.float64)
@@ -296,6 +305,7 @@ class Reference:
         self.R.ref_adm.argtypes = [REF_VECFUNC, _dp, C.c_int, C.c_int, C.c_int,
                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]
         self.R.ref_gaussj_root.argtypes = [_dp, C.c_int, _dp, C.c_int]
+        self.D.ref_spline_chen.argtypes = [_dp, _dp, _dp, _dp, C.c_int, C.c_int, _dp]
 
     @staticmethod
     def available() -> bool:
@@ -304,6 +314,15 @@ class Reference:
     def romint(self, f, m, hh):
         f = np.ascontiguousarray(f, dtype=np.float64)
         return self.D.ref_romint(_ptr(f), m, hh)
+
+    def spline(self, x, y, xp, m=None):
+        """The reference's spline_chen itself: (rc, yp)."""
+        x, y, xp = (np.array(v, dtype=np.float64) for v in (x, y, xp))
+        yp = np.empty(len(xp))
+        mm = None if m is None else np.array([m], dtype=np.float64)
+        rc = self.D.ref_spline_chen(_ptr(x), _ptr(y), _ptr(xp), _ptr(yp), len(x), len(xp),
+                                    None if mm is None else _ptr(mm))
+        return rc, yp
 
     def gaussj(self, a, b, variant="dealii"):
         a = np.array(a, dtype=np.float64, order="C")

@@ -3,8 +3,8 @@
 // Links the reference's own DEALII_SCFT/src NR routines, compiled from source
 // as C++ the way DEALII_SCFT/CMakeLists.txt:36 compiles them, and exposes them
 // with C linkage for the tests: adm_chen (ADM_chen_C.c:18), broydn
-// (DEALII_SCFT/src/broydn.c:44), romint (romint.c:21) and gaussj
-// (DEALII_SCFT/src/gaussj.c:7).  The reference calls exit() on errors
+// (DEALII_SCFT/src/broydn.c:44), romint (romint.c:21), gaussj
+// (DEALII_SCFT/src/gaussj.c:7) and spline_chen (spline_chen.c:13).  The reference calls exit() on errors
 // (nrutil.c:16-23, romint.c:31, ADM_chen_C.c:65); the recipe redirects exit to
 // __wrap_exit at link time so that an error unwinds back here.
 #include <csetjmp>
@@ -114,6 +114,22 @@ int ref_gaussj_dealii(double *a, int n, double *b, int m) {
   }
   free_dmatrix(A, 1, n, 1, n);
   free_dmatrix(B, 1, n, 1, m);
+  return rc;
+}
+
+
+// spline_chen (spline_chen.c:13-106): m == NULL selects the not-a-knot end
+// condition.  Returns 0, or -(100+code) when the reference called exit(code).
+int ref_spline_chen(double *x, double *y, double *xp, double *yp, int nx, int nxp, double *m) {
+  int rc = 0;
+  int j = setjmp(g_jb);
+  if (j == 0) {
+    g_armed = 1;
+    spline_chen(x, y, xp, yp, nx, nxp, m);
+  } else {
+    rc = -j;
+  }
+  g_armed = 0;
   return rc;
 }
 

@@ -1092,3 +1092,66 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
   free(mem);
   return rc;
 }
+
+/* ------------------------------------------------------------------------- */
+/* cubic spline transfer (spline_chen.c:13-106)                               */
+/* ------------------------------------------------------------------------- */
+int or_spline(const double *x, const double *y, int nx, const double *xp, double *yp, int nxp, const double *m) {
+  if (nx < 2 || (!m && nx <= 3)) return -1;
+  for (int i = 1; i < nx; i++)
+    if (!(x[i] > x[i - 1])) return -2;
+  double *lo = (double *)calloc((size_t)nx, sizeof(double)), *di = (double *)calloc((size_t)nx, sizeof(double));
+  double *up = (double *)calloc((size_t)nx, sizeof(double)), *rh = (double *)calloc((size_t)nx, sizeof(double));
+  if (!lo || !di || !up || !rh) { free(lo); free(di); free(up); free(rh); return -3; }
+  /* interior rows i = 1..nx-2 (0-based): h_{i-1}/6 M_{i-1} + (h_{i-1}+h_i)/3 M_i + h_i/6 M_{i+1} = slope jump */
+  for (int i = 1; i < nx - 1; i++) {
+    double a = x[i] - x[i - 1], b = x[i + 1] - x[i];
+    lo[i] = a / 6.0;
+    di[i] = (x[i + 1] - x[i - 1]) / 3.0;
+    up[i] = b / 6.0;
+    rh[i] = (y[i + 1] - y[i]) / b - (y[i] - y[i - 1]) / a;
+  }
+  /* The end values M0, M_{nx-1} are eliminated from the inner rows 1 and nx-2:
+     M = m at both ends, or the not-a-knot conditions
+     M0 = (1 + h0/h1) M1 - (h0/h1) M2  and its mirror at the right end; the
+     inner system for M1..M_{nx-2} is then swept by Thomas. */
+  double *M = (double *)calloc((size_t)nx, sizeof(double));
+  if (!M) { free(lo); free(di); free(up); free(rh); return -3; }
+  const int a = 1, b = nx - 2; /* inner rows */
+  double rl = 0.0, rr = 0.0;   /* not-a-knot ratios h0/h1 and g1/g0 */
+  if (m) {
+    M[0] = M[nx - 1] = *m;
+    if (b >= a) { rh[a] -= lo[a] * *m; rh[b] -= up[b] * *m; }
+  } else {
+    rl = (x[1] - x[0]) / (x[2] - x[1]);
+    rr = (x[nx - 1] - x[nx - 2]) / (x[nx - 2] - x[nx - 3]);
+    di[a] += lo[a] * (1.0 + rl);
+    up[a] -= lo[a] * rl;
+    di[b] += up[b] * (1.0 + rr);
+    lo[b] -= up[b] * rr;
+  }
+  for (int i = a + 1; i <= b; i++) {
+    double w = lo[i] / di[i - 1];
+    di[i] -= w * up[i - 1];
+    rh[i] -= w * rh[i - 1];
+  }
+  if (b >= a) {
+    M[b] = rh[b] / di[b];
+    for (int i = b - 1; i >= a; i--) M[i] = (rh[i] - up[i] * M[i + 1]) / di[i];
+  }
+  if (!m) {
+    M[0] = (1.0 + rl) * M[1] - rl * M[2];
+    M[nx - 1] = (1.0 + rr) * M[nx - 2] - rr * M[nx - 3];
+  }
+  for (int k = 0; k < nxp; k++) {
+    int klo = 0, khi = nx - 1;
+    while (khi - klo > 1) {
+      int c = (khi + klo) >> 1;
+      if (x[c] > xp[k]) khi = c; else klo = c;
+    }
+    double h = x[khi] - x[klo], a = (x[khi] - xp[k]) / h, b = (xp[k] - x[klo]) / h;
+    yp[k] = a * y[klo] + b * y[khi] + ((a * a * a - a) * M[klo] + (b * b * b - b) * M[khi]) * (h * h) / 6.0;
+  }
+  free(lo); free(di); free(up); free(rh); free(M);
+  return 0;
+}

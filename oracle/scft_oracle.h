@@ -113,6 +113,17 @@ typedef struct or_mix_opts {
 } or_mix_opts;
 int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int *iters, double *err);
 
+/* Cubic spline of the table (x, y) (nx points, x increasing) evaluated at the
+   nxp points xp into yp: spline_chen.c:13-106.  m == NULL: not-a-knot end
+   conditions (the third derivative is continuous at the second and second-last
+   points; nx > 3); otherwise the second derivative is *m at both ends.  The
+   second derivatives solve the same equations as the reference's dense system,
+   here with the end values eliminated into the inner rows and a Thomas sweep.
+   Points outside [x0, x_{nx-1}] take the end cubic (extrapolation), as the
+   reference's bisection does.  Returns 0, -1 for nx too small, -2 for x not
+   strictly increasing. */
+int or_spline(const double *x, const double *y, int nx, const double *xp, double *yp, int nxp, const double *m);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,8 @@ SIGNATURES = {
     "scft_batch_destroy": (C.c_int, [C.c_void_p]),
     "scft_kernel_launches": (C.c_longlong, []),
     "scft_mem_trim": (C.c_longlong, []),
+    "scft_refine_bisect": (C.c_int, [C.c_int, _dp, _dp]),
+    "scft_spline": (C.c_int, [C.c_int, C.POINTER(C.c_int), _dp, _dp, C.POINTER(C.c_int), _dp, _dp, _dp]),
     "scft_batch_solve_async": (C.c_int, [C.c_void_p, C.POINTER(ScftSolveOpts)]),
     "scft_batch_wait": (C.c_int, [C.c_void_p, C.POINTER(ScftResult)]),
     "scft_batch_evaluate_scheme": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),

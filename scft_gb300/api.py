@@ -162,6 +162,42 @@ def read_res(path: str, max_rows: int = 1 << 20):
 
 
 # ---------------------------------------------------------------------------
+# mesh refinement and field transfer (refine_mesh of the deal.II driver)
+# ---------------------------------------------------------------------------
+def refine_bisect(x):
+    """Every element of the mesh cut in two (scft.cc:132-166)."""
+    xa = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty(2 * len(xa) - 1)
+    check(L.load().scft_refine_bisect(len(xa), _dp(xa), _dp(out)), "scft_refine_bisect")
+    return out
+
+
+def spline(tables, m=None):
+    """Cubic splines on the GPU: tables is a sequence of (x, y, xp); returns
+    the list of yp (spline_chen.c:13-106; m None = not-a-knot ends)."""
+    nx = (C.c_int * len(tables))(*[len(t[0]) for t in tables])
+    npt = (C.c_int * len(tables))(*[len(t[2]) for t in tables])
+    x = np.ascontiguousarray(np.concatenate([np.asarray(t[0], dtype=np.float64) for t in tables]))
+    y = np.ascontiguousarray(np.concatenate([np.asarray(t[1], dtype=np.float64) for t in tables]))
+    xp = np.ascontiguousarray(np.concatenate([np.asarray(t[2], dtype=np.float64) for t in tables]))
+    yp = np.empty(len(xp))
+    mm = None if m is None else np.array([m], dtype=np.float64)
+    check(L.load().scft_spline(len(tables), nx, _dp(x), _dp(y), npt, _dp(xp), _dp(yp), _dp(mm)), "scft_spline")
+    off = np.concatenate([[0], np.cumsum([len(t[2]) for t in tables])])
+    return [yp[off[i]:off[i + 1]] for i in range(len(tables))]
+
+
+def transfer_field(x, w, x_new):
+    """refine_mesh's transfer of a nodal field to a new mesh: the interior values
+    through the not-a-knot spline of the interior table, the wall values kept."""
+    x, w, x_new = (np.asarray(v, dtype=np.float64) for v in (x, w, x_new))
+    out = np.empty(len(x_new))
+    out[1:-1] = spline([(x[1:-1], w[1:-1], x_new[1:-1])])[0]
+    out[0], out[-1] = w[0], w[-1]
+    return out
+
+
+# ---------------------------------------------------------------------------
 # solvers
 # ---------------------------------------------------------------------------
 def adm(x, n, f, flag=0, maxit=1000000):

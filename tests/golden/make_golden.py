@@ -162,6 +162,31 @@ def fixtures_scft_mixing(O, R):
     })
 
 
+def fixtures_spline(R):
+    """spline_chen (spline_chen.c:13-106) compiled from the reference: the field
+    transfer of refine_mesh (scft.cc:162-163) on a bisected mesh, and random
+    tables with every end condition, extrapolation included."""
+    cases = []
+    g = json.load(open(os.path.join(HERE, "dealii_N33.json")))
+    x = np.array(g["x"]); w = np.array(g["w"])
+    xn = np.empty(2 * len(x) - 1); xn[0::2] = x; xn[1::2] = 0.5 * (x[:-1] + x[1:])
+    rc, yp = R.spline(x[1:-1], w[1:-1], xn[1:-1])
+    cases.append({"name": "refine_mesh N=33 -> 65", "x": x[1:-1].tolist(), "y": w[1:-1].tolist(),
+                  "xp": xn[1:-1].tolist(), "m": None, "rc": rc, "yp": yp.tolist()})
+    rng = np.random.default_rng(7)
+    for nx, m in ((4, None), (7, 0.0), (40, None), (40, -2.5), (129, None)):
+        xs = np.sort(rng.uniform(0.0, 6.0, nx))
+        ys = np.cos(xs) + 0.05 * rng.normal(size=nx)
+        xp = np.concatenate([np.linspace(xs[0] - 0.5, xs[-1] + 0.5, 61), xs])
+        rc, yp = R.spline(xs, ys, xp, m)
+        cases.append({"name": f"random nx={nx} m={m}", "x": xs.tolist(), "y": ys.tolist(), "xp": xp.tolist(),
+                      "m": m, "rc": rc, "yp": yp.tolist()})
+    rc, _ = R.spline([0.0, 1.0, 2.0], [0.0, 1.0, 0.0], [0.5])
+    cases.append({"name": "not-a-knot with 3 points", "x": [0.0, 1.0, 2.0], "y": [0.0, 1.0, 0.0], "xp": [0.5],
+                  "m": None, "rc": rc, "yp": None})
+    dump("spline.json", {"source": "DEALII_SCFT/src/spline_chen.c compiled from the reference", "cases": cases})
+
+
 def main():
     orc.build(with_reference=True)
     O = orc.Oracle()
@@ -169,6 +194,7 @@ def main():
     fixtures_fields(O)
     fixtures_routines(R)
     fixtures_scft_mixing(O, R)
+    fixtures_spline(R)
     print("golden fixtures written to", HERE)
 
 

@@ -212,3 +212,29 @@ def test_live_reference_matches_restatement(oracle, reference):
     rc2, x2, _ = reference.adm_chen(toy3, [1.0, 2.0, 3.0], 1e-12, 5000, 0.9, 5)
     assert rc == rc2
     np.testing.assert_allclose(x, x2, rtol=1e-9)
+
+
+def test_spline_restatement_matches_reference_fixture(oracle):
+    """spline_chen.c:13-106 restated (banded solve) against the reference's own
+    routine: the refine_mesh transfer N=33 -> 65 and random tables with every
+    end condition, extrapolation included; the 3-point not-a-knot call the
+    reference exits on is refused."""
+    for c in load("spline.json")["cases"]:
+        rc, yp = oracle.spline(c["x"], c["y"], c["xp"], c["m"])
+        if c["rc"] != 0:
+            assert rc != 0, c["name"]
+            continue
+        assert rc == 0, c["name"]
+        np.testing.assert_allclose(yp, c["yp"], rtol=1e-12, atol=1e-12 * np.abs(c["yp"]).max(), err_msg=c["name"])
+
+
+def test_spline_restatement_matches_live_reference(oracle, reference):
+    rng = np.random.default_rng(11)
+    for nx in (4, 9, 64):
+        x = np.sort(rng.uniform(-1, 3, nx))
+        y = np.exp(-x * x) + 0.01 * rng.normal(size=nx)
+        xp = np.linspace(x[0] - 0.2, x[-1] + 0.2, 33)
+        for m in (None, 0.0, 0.7):
+            a = oracle.spline(x, y, xp, m)[1]
+            b = reference.spline(x, y, xp, m)[1]
+            np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-13)
