@@ -106,7 +106,9 @@ void scft_adm_set_maxit(int maxit);
 
 /* Replaces adm_chen (DEALII_SCFT/src/ADM_chen_C.c:18-147): Anderson mixing for
    F(x) = 0, 0-based.  Returns 0 solved, 1 not solved, 2 NaN residual, <0 error.
-   f == scft_fem_residual0_vf keeps every evaluation on the device. */
+   The history depth min(nn, n) may be up to 63 (the deal.II driver uses up to
+   50, drivescft.cc:296).  f == scft_fem_residual0_vf keeps every evaluation on
+   the device. */
 int scft_adm_chen(scft_vecfunc f, double *x, double tol, int maxit, int n, double lmd, int nn,
                   int final_);
 

@@ -12,6 +12,9 @@ namespace scft {
 
 constexpr int MIX_THREADS = 256;
 constexpr int MAXD = MIX_MAXD;
+// history limit of the drop-in adm_chen (the deal.II driver asks for up to 50,
+// drivescft.cc:296): U (m x m) and V live in shared memory
+constexpr int ADM_MAXD = 64;
 
 // block-wide max of v (all threads receive it)
 __device__ double block_max(double v, double *sm) {
@@ -47,7 +50,7 @@ cudaError_t mix_launch(const MixDev &m, cudaStream_t st) {
 // mode 0: zero pivot += 1e-18 (gaussj.c:38); mode 1: return 1
 // (DEALII_SCFT/src/gaussj.c:45-50).  a: n x n, b: n x 1, row-major.
 __device__ int dev_gaussj(double *a, int n, double *b, int mode) {
-  int ipiv[MAXD], indxr[MAXD], indxc[MAXD];
+  int ipiv[ADM_MAXD], indxr[ADM_MAXD], indxc[ADM_MAXD];
   for (int j = 0; j < n; j++) ipiv[j] = 0;
   for (int i = 0; i < n; i++) {
     double big = 0.0;
@@ -96,7 +99,7 @@ __device__ int dev_gaussj(double *a, int n, double *b, int mode) {
 // ADM_chen_C.c:55-135, one iteration k: Y_k = f(X_k) is already in Y.
 __global__ void __launch_bounds__(MIX_THREADS) admchen_step_kernel(AdmChenDev a) {
   __shared__ double sm[32];
-  __shared__ double U[MAXD * MAXD], V[MAXD];
+  __shared__ double U[ADM_MAXD * ADM_MAXD], V[ADM_MAXD];
   __shared__ int sh_m, sh_fail;
   const int tid = threadIdx.x, n = a.n, D = a.depth;
   const int k = *a.k;
@@ -169,7 +172,7 @@ __global__ void __launch_bounds__(MIX_THREADS) admchen_step_kernel(AdmChenDev a)
 }
 
 cudaError_t admchen_step_launch(const AdmChenDev &a, cudaStream_t st) {
-  if (a.nm > MAXD - 1) return cudaErrorInvalidValue;
+  if (a.nm > ADM_MAXD - 1) return cudaErrorInvalidValue;
   admchen_step_kernel<<<1, MIX_THREADS, 0, st>>>(a);
   return cudaGetLastError();
 }

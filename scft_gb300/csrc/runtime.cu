@@ -44,6 +44,9 @@ static cudaError_t solve_dispatch(int C, int NW, const BatchDev &b, const ClassD
 long long seq_scratch_doubles(int n, int nsteps);
 cudaError_t seq_propagate_launch(const BatchDev &b, int scheme, int wmode, double *scratch, const long long *off,
                                  cudaStream_t st);
+int seq_block_max_nodes();
+cudaError_t seq_block_launch(const BatchDev &b, int max_nodes, int scheme, int wmode, double *scratch,
+                             const long long *off, cudaStream_t st);
 
 static int solve_ctas_per_sm(int C, int NW) {
   int n = 0;
@@ -662,7 +665,13 @@ static int seq_enqueue(scft_batch *B, int scheme, int wmode) {
     if ((rc = dalloc(&B->d_seq, (size_t)tot)) || (rc = dalloc(&B->d_seq_off, (size_t)B->count))) return rc;
     CK(cudaMemcpyAsync(B->d_seq_off, off.data(), B->count * sizeof(long long), cudaMemcpyHostToDevice, B->st));
   }
-  CK(seq_propagate_launch(batch_dev(B), scheme, wmode, B->d_seq, B->d_seq_off, B->st));
+  // block-parallel form when every instance's coefficients fit in one CTA's
+  // shared memory, the one-thread form otherwise
+  const int maxn = *std::max_element(B->n.begin(), B->n.end());
+  if (maxn <= seq_block_max_nodes())
+    CK(seq_block_launch(batch_dev(B), maxn, scheme, wmode, B->d_seq, B->d_seq_off, B->st));
+  else
+    CK(seq_propagate_launch(batch_dev(B), scheme, wmode, B->d_seq, B->d_seq_off, B->st));
   g_launches++;
   return SCFT_OK;
 }
@@ -1492,7 +1501,7 @@ int scft_adm_chen(scft_vecfunc f, double *x, double tol, int maxit, int n, doubl
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   if (!f || !x || n <= 0 || maxit < 0 || nn < 0) return set_err(SCFT_EINVAL, "scft_adm_chen");
   const int nm = std::min(nn, n);
-  if (nm > 15) return set_err(SCFT_EINVAL, "scft_adm_chen: history depth %d exceeds 15", nm);
+  if (nm > 63) return set_err(SCFT_EINVAL, "scft_adm_chen: history depth %d exceeds 63", nm);
   const bool internal = (f == scft_fem_residual0_vf) && g_drop.set && n == g_drop.n - 2;
   const int depth = nm + 1;
   cudaStream_t st;

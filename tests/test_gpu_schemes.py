@@ -84,3 +84,19 @@ def test_dealii_golden_field_through_the_drop_in(oracle):
     phi_ref, q_ref = oracle.propagate(p, w)
     assert rel(phi, phi_ref) <= TOL64 and abs(Q - q_ref) <= TOL64 * abs(q_ref)
     api.set_config(f0, x=x)  # back to the default drop-in configuration
+
+
+def test_one_thread_form_for_instances_beyond_shared_memory(oracle):
+    """Instances too large for the block-parallel form (coefficients in one CTA's
+    shared memory, about 2200 nodes) run the one-thread form; both match the
+    oracle."""
+    d = W.instance(2400, 6.0, 32, 5, 0)
+    ws = fields([d], 13)
+    with api.Batch([d]) as b:
+        b.set_fields(ws)
+        b.evaluate_scheme(SCHEME_IRK2, W_CONSISTENT)
+        _, phi, Q = b.get()
+    p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d["rule"], wmode=W_CONSISTENT,
+                          scheme=SCHEME_IRK2, wall_w=[ws[0][0], ws[0][-1]])
+    phi_ref, q_ref = oracle.propagate(p, ws[0])
+    assert rel(phi[0], phi_ref) <= TOL64 and abs(Q[0] - q_ref) <= TOL64 * abs(q_ref)
