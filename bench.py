@@ -347,7 +347,11 @@ def ours_arm(args):
                    "start": ("learned warm start (conv net, weights " + os.path.relpath(args.weights, ROOT) + ")")
                    if ws is not None else "cold (w0 ~ U[-0.1, 0.1])",
                    "l2": "working set (half-contour stores of concurrent instances) larger than L2",
-                   "mixing": "Anderson depth 10, beta 1.0, ln-residual with (1 - 0.6 d2/dx2) preconditioner",
+                   "mixing": "Anderson depth 10, beta 1.0, ln-residual with (1 - 0.6 d2/dx2) preconditioner; "
+                             f"instances still running after {opts.fork_at} updates fork into {opts.forks} paths "
+                             f"(beta x {', '.join(str(opts.fork_scale[k]) for k in range(opts.forks))}), own path "
+                             f"kept if converged by update {opts.fork_at + opts.fork_grace}, else the path with "
+                             "the fewest iterations",
                    "parallelism": f"replicas x{world}, batch split by cost"},
         "gpu_launches": launches,
         "iterations_mean": statistics.mean(iters),
@@ -358,7 +362,7 @@ def ours_arm(args):
         "converged_per_step": conv_all,
         "status_last_step": {name: int(((r["status"] & bit) != 0).sum()) for name, bit in
                              (("converged", 4), ("max_iterations", 8), ("non_finite", 2), ("not_dominant", 1),
-                              ("restarted", 16), ("watchdog", 32))},
+                              ("restarted", 16), ("watchdog", 32), ("forked_winner", 128))},
         "clocks": clk,
         "roofline": roofline,
     }

@@ -33,6 +33,8 @@ extern "C" {
 #define SCFT_ST_RESTARTED 16   /* the Anderson history was restarted at least once */
 #define SCFT_ST_WATCHDOG 32    /* the host loop stopped on its launch cap */
 #define SCFT_ST_FP64 64        /* the FP32 iteration stalled and the FP64 propagator finished the solve */
+#define SCFT_ST_FORKED 128     /* the result comes from a forked path of the mixing (scft_solve_opts.forks) */
+#define SCFT_MAX_FORKS 4
 
 enum { SCFT_RULE_ROMBERG = 0, SCFT_RULE_TRAPEZOID = 1 };
 enum { SCFT_F32 = 0, SCFT_F64 = 1 };
@@ -171,6 +173,18 @@ typedef struct scft_solve_opts {
   double budget_ms;   /* > 0: device-side time budget of the solve; a thread group that finds it
                          spent at an iteration boundary stops its instance with SCFT_ST_WATCHDOG
                          (the solve returns normally); 0: none */
+  int forks;          /* fused FP32 solves: an instance still running after fork_at iterations is
+                         copied into `forks` (<= SCFT_MAX_FORKS) further paths whose mixing parameter
+                         is beta times fork_scale[r]; thread groups that have run out of instances
+                         take these paths.  The instance's own path wins if it converges within
+                         fork_at + fork_grace iterations; otherwise the path that converges in the
+                         fewest iterations wins (ties: the lowest path, the instance itself first).
+                         The outcome does not depend on timing; paths stop once they cannot win.
+                         The iteration count is the winner's, SCFT_ST_FORKED marks a forked winner.
+                         0: off.  Not used with finish_stall > 0 */
+  int fork_at;
+  int fork_grace;
+  double fork_scale[4];
 } scft_solve_opts;
 
 typedef struct scft_result {

@@ -7,9 +7,9 @@ interface over that ABI.  Importing the package does not load the library;
 has not been built.
 """
 from ._lib import (F32, F64, MIX_LINEAR, MIX_LOG, RULE_ROMBERG, RULE_TRAPEZOID, SCHEME_IE, SCHEME_IRK2,
-                   ST_CONVERGED, ST_MAXIT, ST_NONFINITE, ST_NOT_DOMINANT, ST_RESTARTED, ST_WATCHDOG,
-                   W_CONSISTENT, W_ROWSCALED, ScftError, load)
+                   ST_CONVERGED, ST_FORKED, ST_FP64, ST_MAXIT, ST_NONFINITE, ST_NOT_DOMINANT, ST_RESTARTED,
+                   ST_WATCHDOG, W_CONSISTENT, W_ROWSCALED, ScftError, load)
 
 __all__ = ["F32", "F64", "MIX_LINEAR", "MIX_LOG", "RULE_ROMBERG", "RULE_TRAPEZOID", "SCHEME_IE", "SCHEME_IRK2",
-           "ST_CONVERGED", "ST_MAXIT", "ST_NONFINITE", "ST_NOT_DOMINANT", "ST_RESTARTED", "ST_WATCHDOG",
-           "W_CONSISTENT", "W_ROWSCALED", "ScftError", "load"]
+           "ST_CONVERGED", "ST_FORKED", "ST_FP64", "ST_MAXIT", "ST_NONFINITE", "ST_NOT_DOMINANT", "ST_RESTARTED",
+           "ST_WATCHDOG", "W_CONSISTENT", "W_ROWSCALED", "ScftError", "load"]

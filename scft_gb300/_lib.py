@@ -26,6 +26,9 @@ ST_CONVERGED = 4
 ST_MAXIT = 8
 ST_RESTARTED = 16
 ST_WATCHDOG = 32
+ST_FP64 = 64
+ST_FORKED = 128
+MAX_FORKS = 4
 
 RULE_ROMBERG, RULE_TRAPEZOID = 0, 1
 F32, F64 = 0, 1
@@ -57,7 +60,9 @@ class ScftSolveOpts(C.Structure):
                 ("residual_mode", C.c_int), ("precond", C.c_double), ("iters_per_graph", C.c_int),
                 ("beta_schedule", C.c_int), ("weighted", C.c_int), ("step_cap", C.c_double),
                 ("field_floor", C.c_double), ("fused", C.c_int),
-                ("finish_stall", C.c_int), ("finish_tol", C.c_double), ("budget_ms", C.c_double)]
+                ("finish_stall", C.c_int), ("finish_tol", C.c_double), ("budget_ms", C.c_double),
+                ("forks", C.c_int), ("fork_at", C.c_int), ("fork_grace", C.c_int),
+                ("fork_scale", C.c_double * 4)]
 
 
 class ScftResult(C.Structure):

@@ -62,6 +62,12 @@ struct scft_batch {
   int live_cap = 0, live_maxc = 0;
   std::vector<double> live_ms[2], live_units[2];
   std::vector<long long> live_launches[2];
+  // forked paths: per-path arrays (w, phi, Q, status, active and the Anderson
+  // state) hold 1 + paths copies; d_win per instance; d_fork the per-class fork
+  // queues (4 control ints + one entry per instance), initialised from h_fork
+  int paths = 0;
+  int *d_win = nullptr, *d_fork = nullptr, *h_fork = nullptr;
+  size_t fork_cap = 0;
   // a fused solve enqueued by scft_batch_solve_async, completed by scft_batch_wait
   bool pending = false;
   scft_solve_opts pending_opts{};

@@ -21,7 +21,16 @@ struct BatchDev {
                            // sample index (v = min(ctz(k), 14)), [15] for k = 0 and k = nsteps
   const int *active;       // nonzero: evaluate this instance
   int *status;             // per-instance status bits (SCFT_ST_*)
+  // Forked solve paths: id v = r * base + i is path r of instance i (r = 0 the
+  // instance itself).  Static data (n, nsteps, ds, x, qw, node_off) is read at
+  // i, the field, density and Q of path r at node_off[i] + r * rep_nodes, and
+  // active / status / Q at v.  base = 0: no forks, v = i.
+  int base = 0;
+  long long rep_nodes = 0;
 };
+
+// Path and instance of id v (see BatchDev::base).
+__host__ __device__ __forceinline__ int path_of(int v, int base) { return base ? v / base : 0; }
 
 // One shape class (C nodes per thread, NW warps per instance) of a batch.
 struct ClassDev {
@@ -33,6 +42,11 @@ struct ClassDev {
   int workers;             // number of slots
   int want;                // evaluate instances whose active flag equals this value
   unsigned long long *work = nullptr;  // if set: += n (nsteps/2 + 1) per instance evaluated
+  // Forked paths of the fused solve (MixDev::forks > 0): fork_ctl = {published
+  // forks, claimed path jobs, instances that may still fork}; fork_list[k] =
+  // 1 + the instance of the k-th published fork (0: not yet written).
+  int *fork_ctl = nullptr;
+  int *fork_list = nullptr;
 };
 
 // Status bits written by the kernels.
@@ -44,6 +58,7 @@ enum : int {
   ST_RESTARTED = 16,
   ST_WATCHDOG = 32,
   ST_FP64 = 64,
+  ST_FORKED = 128,         // the result comes from a forked path of the mixing
 };
 
 }  // namespace scft

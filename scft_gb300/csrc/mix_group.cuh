@@ -68,6 +68,7 @@ struct MixSmem {
   int slot[MIX_MAXD];
   int ctl[4];
   int stop;
+  int forked;   // set by mix_step when this update copied the instance into its forked paths
 };
 
 // Group-wide max of v (every thread of the group receives it).
@@ -82,6 +83,12 @@ __device__ __forceinline__ double group_max(double v, MixSmem<NW> &S, int tid, S
   return warp_max(r);
 }
 
+// Key of path r converging after `it` updates (see MixDev::win): the instance's
+// own path (r = 0) within the grace iterations after the fork beats every path.
+__device__ __forceinline__ int fork_key(const MixDev &m, int it, int r) {
+  return (r == 0 && it <= m.fork_at + m.fork_grace) ? 0 : it * 16 + r;
+}
+
 // One Anderson iteration of instance `inst` by threads tid = 0 .. 32*NW-1 of a
 // group; `sync` is the group's barrier.  Returns true (in every thread) when the
 // instance is finished: converged (or handed to the FP64 check), non-finite, or
@@ -92,13 +99,15 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
   constexpr int NT = 32 * NW;
   const int lane = tid & 31, wid = tid >> 5;
   const int act = m.active[inst];
-  const int n = m.n[inst], N = n - 2;
-  const long long no = m.node_off[inst], io = m.int_off[inst];
-  const double *x = m.x + no, *f0 = m.f0 + no, *phi = m.phi + no;
-  double *w = m.w + no;
-  double *graw = m.graw + io, *gcur = m.gcur + io, *gprev = m.gprev + io, *wprev = m.wprev + io;
+  const int r = path_of(inst, m.base), ii = inst - r * m.base;  // path and instance
+  const int n = m.n[ii], N = n - 2;
+  const long long no = m.node_off[ii], io = m.int_off[ii];
+  const long long dno = no + r * m.rep_nodes, dio = io + r * m.rep_int;
+  const double *x = m.x + no, *f0 = m.f0 + no, *phi = m.phi + dno;
+  double *w = m.w + dno;
+  double *graw = m.graw + dio, *gcur = m.gcur + dio, *gprev = m.gprev + dio, *wprev = m.wprev + dio;
   const int D = m.depth;
-  double *hdx = m.hdx + io * D, *hdg = m.hdg + io * D;
+  double *hdx = m.hdx + dio * D, *hdg = m.hdg + dio * D;
   double *G = m.gram + (long long)inst * D * D;
 
   // 1. residual, its norm, raw mixing residual
@@ -129,7 +138,11 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     if (tid == 0) {
       m.err[inst] = e;
       if (act == 1 && m.verify64) m.active[inst] = 2;
-      else { m.status[inst] |= ST_CONVERGED; m.active[inst] = 0; }
+      else {
+        m.status[inst] |= ST_CONVERGED;
+        m.active[inst] = 0;
+        if (m.win) atomicMin(m.win + ii, fork_key(m, it, r));
+      }
     }
     return true;
   }
@@ -137,12 +150,24 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     if (tid == 0) { m.status[inst] |= ST_MAXIT; m.active[inst] = 0; m.err[inst] = e; }
     return true;
   }
-  // time budget: one thread reads the clock, the whole group follows its decision
-  if (m.deadline) {
-    if (tid == 0) S.stop = global_ns() > __ldcg(m.deadline) ? 1 : 0;
+  // time budget, and forked paths that can no longer win (the earliest they
+  // could converge is the next evaluation): one thread decides, the whole
+  // group follows
+  if (m.deadline || m.win) {
+    if (tid == 0) {
+      int stop = 0;
+      if (m.deadline && global_ns() > __ldcg(m.deadline)) stop = 1;
+      else if (m.win && fork_key(m, it + 1, r) > *(volatile const int *)(m.win + ii)) stop = 2;
+      S.stop = stop;
+    }
     sync();
-    if (S.stop) {
-      if (tid == 0) { m.status[inst] |= ST_WATCHDOG; m.active[inst] = 0; m.err[inst] = e; }
+    const int stop = S.stop;
+    if (stop) {
+      if (tid == 0) {
+        if (stop == 1) m.status[inst] |= ST_WATCHDOG;
+        m.active[inst] = 0;
+        m.err[inst] = e;
+      }
       return true;
     }
   }
@@ -244,8 +269,12 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
   //    f0-weighted max norm is <= clip and no node moves by more than
   //    step_cap / ds; the field is kept >= -field_floor / ds.
   const double beta = 1.0 - m.lk[inst];
-  const double dsi = m.ds[inst];
-  double dm = 0.0, da = 0.0;
+  const double dsi = m.ds[ii];
+  // forked paths of this update (instance paths only, at update number fork_at):
+  // path f + 1 steps by d + beta (fork_scale[f] - 1) p, p the preconditioned
+  // residual, i.e. with its own mixing parameter; staged in its own wprev
+  const int nf = (m.forks > 0 && r == 0 && it + 1 == m.fork_at) ? min(m.forks, 4) : 0;
+  double dm = 0.0, da = 0.0, dmf[4] = {0.0, 0.0, 0.0, 0.0}, daf[4] = {0.0, 0.0, 0.0, 0.0};
   for (int j = tid; j < N; j += NT) {
     const double gc = gcur[j];
     double lap = 0.0;
@@ -253,17 +282,40 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
       const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
       lap = ((gc - gcur[j - 1]) / a1 + (gc - gcur[j + 1]) / a2) / (0.5 * (a1 + a2));
     }
-    double d = beta * (gc + m.precond * lap);
+    const double pr = gc + m.precond * lap;
+    double d = beta * pr;
     for (int t = 0; t < cnt; t++) d -= S.gam[t] * hdx[(long long)S.slot[t] * N + j];
     wprev[j] = d;  // staged; wprev receives the old field below
     const double wj = m.weighted ? f0[j + 1] * winv : 1.0;
     dm = fmax(dm, fabs(d) * wj);
     da = fmax(da, fabs(d));
+#pragma unroll
+    for (int f = 0; f < 4; f++)
+      if (f < nf) {
+        const double df = d + beta * (m.fork_scale[f] - 1.0) * pr;
+        m.wprev[io + (f + 1) * m.rep_int + j] = df;
+        dmf[f] = fmax(dmf[f], fabs(df) * wj);
+        daf[f] = fmax(daf[f], fabs(df));
+      }
   }
+  // the step is scaled so that its f0-weighted max norm is <= clip and no node
+  // moves by more than step_cap / ds
+  auto step_scale = [&](double vm, double va) {
+    double sc = (vm > m.clip) ? m.clip / vm : 1.0;
+    if (m.step_cap > 0.0 && va * sc * dsi > m.step_cap) sc = m.step_cap / (va * dsi);
+    return sc;
+  };
   dm = group_max(dm, S, tid, sync);
   da = group_max(da, S, tid, sync);
-  double scale = (dm > m.clip) ? m.clip / dm : 1.0;
-  if (m.step_cap > 0.0 && da * scale * dsi > m.step_cap) scale = m.step_cap / (da * dsi);
+  const double scale = step_scale(dm, da);
+  double scf[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int f = 0; f < 4; f++)
+    if (f < nf) {
+      const double vm = group_max(dmf[f], S, tid, sync);
+      const double va = group_max(daf[f], S, tid, sync);
+      scf[f] = step_scale(vm, va);
+    }
   const double wfloor = (m.field_floor > 0.0) ? -m.field_floor / dsi : -INFINITY;
   for (int j = tid; j < N; j += NT) {
     const double wo = w[j + 1];
@@ -271,6 +323,43 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     wprev[j] = wo;
     gprev[j] = graw[j];
     w[j + 1] = fmax(wo + scale * d, wfloor);
+#pragma unroll
+    for (int f = 0; f < 4; f++)
+      if (f < nf) {
+        const long long fo = io + (f + 1) * m.rep_int;
+        const double df = m.wprev[fo + j];
+        m.wprev[fo + j] = wo;
+        m.gprev[fo + j] = graw[j];
+        m.w[no + (f + 1) * m.rep_nodes + j + 1] = fmax(wo + scf[f] * df, wfloor);
+      }
+  }
+  if (nf) {
+    // the rest of each forked path's state: history, Gram matrix, wall values
+    // and the scalars of the instance after this update
+    for (int f = 0; f < nf; f++) {
+      const long long fo = io + (f + 1) * m.rep_int;
+      double *hx = m.hdx + fo * D, *hg = m.hdg + fo * D;
+      for (int k = tid; k < D * N; k += NT) { hx[k] = hdx[k]; hg[k] = hdg[k]; }
+      const int v = inst + (f + 1) * m.base;
+      double *Gf = m.gram + (long long)v * D * D;
+      for (int k = tid; k < D * D; k += NT) Gf[k] = G[k];
+      if (tid == 0) {
+        double *wf = m.w + no + (f + 1) * m.rep_nodes;
+        wf[0] = w[0];
+        wf[n - 1] = w[n - 1];
+        m.iters[v] = it + 1;
+        m.hcount[v] = cnt;
+        m.hhead[v] = S.ctl[1];
+        m.err[v] = e;
+        m.best[v] = m.best[inst];
+        m.ref_err[v] = m.ref_err[inst];
+        m.ref_it[v] = m.ref_it[inst];
+        m.lk[v] = 1.0 - beta * m.fork_scale[f];
+        m.status[v] = m.status[inst];
+        m.active[v] = act;
+      }
+    }
+    __threadfence();  // the forked state is complete before the caller publishes it
   }
   if (tid == 0) {
     m.iters[inst] = it + 1;
@@ -283,6 +372,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
       if (l < 1e-5) l = m.lmd;
       m.lk[inst] = l;
     }
+    S.forked = nf;
   }
   sync();
   return false;

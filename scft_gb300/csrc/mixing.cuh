@@ -44,6 +44,20 @@ struct MixDev {
   // time budget: globaltimer (ns) after which a group stops its instance with
   // ST_WATCHDOG at the next iteration boundary; null: no budget
   const unsigned long long *deadline;
+  // Forked paths (BatchDev::base): static data at instance i, the node arrays
+  // of path r at node_off[i] + r * rep_nodes, the interior arrays at
+  // int_off[i] + r * rep_int (history: depth times that), scalars and the Gram
+  // matrix at id v.  forks > 0: an instance (r = 0) whose update number fork_at
+  // is taken copies its state into paths 1..forks, path r stepping with
+  // fork_scale[r - 1] times the step (and mixing parameter) of the instance.
+  // win[i] = min over converged paths of their key, iterations * 16 + r, or 0
+  // for the instance's own path converging within fork_at + fork_grace
+  // iterations; a path stops once its earliest possible key exceeds win[i].
+  int base = 0;
+  long long rep_nodes = 0, rep_int = 0;
+  int forks = 0, fork_at = 0, fork_grace = 0;
+  double fork_scale[4] = {1.0, 1.0, 1.0, 1.0};
+  int *win = nullptr;
 };
 
 cudaError_t mix_launch(const MixDev &m, cudaStream_t st);

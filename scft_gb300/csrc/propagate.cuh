@@ -46,6 +46,11 @@ namespace scft {
 #ifndef PACKED_BLOCK
 #define PACKED_BLOCK 1
 #endif
+// Longest wait of a group for a claimed forked-path job to be published (ns).
+#ifndef FORK_WAIT_NS
+#define FORK_WAIT_NS 30000000000ull
+#endif
+
 // Minimum resident CTAs per SM the fused solve kernel is compiled for (its
 // register budget); the planner sizes its grid from the occupancy it gets.
 #ifndef SOLVE_MIN_CTAS
@@ -137,33 +142,80 @@ struct Propagator {
   // limit), then takes the next one.  No barrier spans more than the group,
   // so instances with short contours or few iterations never wait for the
   // slow ones.
+  //
+  // Forked paths (m.forks > 0): an instance that takes its update number
+  // m.fork_at copies its state into m.forks further paths (mix_step) and
+  // publishes them here; once the class queue is empty, groups claim path jobs
+  // in publication order and iterate them the same way.  A job claimed before
+  // its fork is published is waited for (bounded: it ends when every instance
+  // of the class has forked or finished, at the time budget, or after
+  // FORK_WAIT_NS); the instances the waiting groups depend on are all held by
+  // running groups, which wait for nothing.
   __device__ static void solve(const BatchDev &b, const ClassDev &cls, const MixDev &m, GroupSmem<R, NW> &S,
                                MixSmem<NW> &MS, int P, int worker, int bar_id) {
     const int lane = P & 31, wid = P >> 5;
     R *slot = reinterpret_cast<R *>(cls.scratch) + (long long)worker * cls.slot_elems;
     auto sync = [&]() { gsync(bar_id); };
-    for (;;) {
-      int item;
+    // value of thread 0 for the whole group
+    auto bcast = [&](int v) -> int {
       if (NW > 1) {
-        if (P == 0) S.item = atomicAdd(cls.head, 1);
+        if (P == 0) S.item = v;
         gsync(bar_id);
-        item = S.item;
+        v = S.item;
         gsync(bar_id);
-      } else {
-        item = 0;
-        if (lane == 0) item = atomicAdd(cls.head, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
+        return v;
       }
+      return __shfl_sync(0xffffffffu, v, 0);
+    };
+    const bool forking = m.forks > 0 && cls.fork_ctl != nullptr;
+    auto run_path = [&](int v) {
+      const int r = path_of(v, b.base), ii = v - r * b.base;
+      // a forked path that can no longer win is not evaluated at all
+      if (r > 0 && bcast(P == 0 && fork_key(m, m.iters[v], r) > *(volatile const int *)(m.win + ii))) return;
+      for (;;) {
+        instance(b, S, P, lane, wid, v, slot, bar_id);
+        if (cls.work && P == 0)
+          atomicAdd(cls.work, (unsigned long long)b.n[ii] * (unsigned long long)(b.nsteps[ii] / 2 + 1));
+        gsync(bar_id);  // density, Q and status of this pass visible to the group
+        if (mix_step<NW>(m, v, P, MS, sync)) break;
+        if (forking && MS.forked && P == 0) {
+          const int k = atomicAdd(cls.fork_ctl, 1);
+          atomicExch(cls.fork_list + k, ii + 1);
+          __threadfence();
+          atomicSub(cls.fork_ctl + 2, 1);
+        }
+      }
+    };
+    for (;;) {
+      const int item = bcast(P == 0 ? atomicAdd(cls.head, 1) : 0);
       if (item >= cls.count) break;
       const int inst = cls.items[item];
-      if (b.active[inst] != cls.want) continue;
-      for (;;) {
-        instance(b, S, P, lane, wid, inst, slot, bar_id);
-        if (cls.work && P == 0)
-          atomicAdd(cls.work, (unsigned long long)b.n[inst] * (unsigned long long)(b.nsteps[inst] / 2 + 1));
-        gsync(bar_id);  // density, Q and status of this pass visible to the group
-        if (mix_step<NW>(m, inst, P, MS, sync)) break;
+      if (b.active[inst] == cls.want) run_path(inst);
+      // an instance that ends before its fork update never forks
+      if (forking && P == 0 && m.iters[inst] < m.fork_at) atomicSub(cls.fork_ctl + 2, 1);
+    }
+    if (!forking) return;
+    for (;;) {
+      int v = -1;
+      if (P == 0) {
+        const int job = atomicAdd(cls.fork_ctl + 1, 1);
+        const int k = job / m.forks, f = job - k * m.forks;
+        if (k < cls.count) {
+          const unsigned long long t0 = global_ns();
+          for (;;) {
+            const int e = *(volatile const int *)(cls.fork_list + k);
+            if (e) { v = (f + 1) * b.base + (e - 1); break; }
+            if (*(volatile const int *)(cls.fork_ctl + 2) <= 0 && k >= *(volatile const int *)cls.fork_ctl) break;
+            const unsigned long long t = global_ns();
+            if ((m.deadline && t > __ldcg(m.deadline)) || t - t0 > FORK_WAIT_NS) break;
+            __nanosleep(4000);
+          }
+          __threadfence();
+        }
       }
+      v = bcast(v);
+      if (v < 0) break;
+      run_path(v);
     }
   }
 
@@ -361,12 +413,13 @@ struct Propagator {
   __device__ static void instance(const BatchDev &b, GroupSmem<R, NW> &S, int P, int lane, int wid,
                                   int inst, R *slot, int bar_id) {
     const unsigned FULL = 0xffffffffu;
-    const int n = b.n[inst], N = n - 2, ns = b.nsteps[inst], half = ns / 2;
-    const double ds = b.ds[inst];
-    const long long off = b.node_off[inst];
+    const int path = path_of(inst, b.base), ii = inst - path * b.base;  // forked path and instance
+    const int n = b.n[ii], N = n - 2, ns = b.nsteps[ii], half = ns / 2;
+    const double ds = b.ds[ii];
+    const long long off = b.node_off[ii], doff = off + path * b.rep_nodes;
     const double *x = b.x + off;
-    const double *w = b.w + off;
-    if (P < 16) S.qw[P] = (R)b.qw[(long long)inst * 16 + P];
+    const double *w = b.w + doff;
+    if (P < 16) S.qw[P] = (R)b.qw[(long long)ii * 16 + P];
     gsync(bar_id);
     int bad = 0;
 
@@ -731,7 +784,7 @@ struct Propagator {
 
     // ---------------- epilogue: phi, Q, status ----------------
     double qpart = 0.0;
-    double *phi = b.phi + off;
+    double *phi = b.phi + doff;
 #pragma unroll
     for (int c = 0; c < C; c++) {
       const int j = P * C + c;

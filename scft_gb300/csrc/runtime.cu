@@ -480,11 +480,37 @@ static void free_mix(scft_batch *B) {
   B->depth = 0;
 }
 
-static int ensure_mix(scft_batch *B, int depth) {
-  if (B->depth == depth) return SCFT_OK;
-  free_mix(B);
-  const size_t ni = (size_t)B->total_int, c = (size_t)B->count;
+// Replace a device array of n_old elements by one of n_new, keeping the first n_old.
+template <typename T>
+static int grow_array(T *&p, size_t n_old, size_t n_new) {
+  T *q = nullptr;
+  int rc = dalloc(&q, n_new);
+  if (rc) return rc;
+  if (p && n_old) CK(cudaMemcpy(q, p, n_old * sizeof(T), cudaMemcpyDeviceToDevice));
+  dfree(p);
+  p = q;
+  return SCFT_OK;
+}
+
+// Anderson state for history depth `depth` and room for `paths` forked paths
+// per instance (the capacity only grows).
+static int ensure_mix(scft_batch *B, int depth, int paths = 0) {
+  paths = std::max(paths, B->paths);
+  if (B->depth == depth && B->paths == paths) return SCFT_OK;
   int rc;
+  if (paths > B->paths) {
+    const size_t no = (size_t)B->total_nodes, c = (size_t)B->count, f0 = 1 + B->paths, f1 = 1 + paths;
+    if ((rc = grow_array(B->d_w, no * f0, no * f1)) || (rc = grow_array(B->d_phi, no * f0, no * f1)) ||
+        (rc = grow_array(B->d_Q, c * f0, c * f1)) || (rc = grow_array(B->d_status, c * f0, c * f1)) ||
+        (rc = grow_array(B->d_active, c * f0, c * f1)))
+      return rc;
+    dfree(B->d_win);
+    if ((rc = dalloc(&B->d_win, c))) return rc;
+  }
+  free_mix(B);
+  B->paths = paths;
+  const size_t f = 1 + (size_t)paths;
+  const size_t ni = (size_t)B->total_int * f, c = (size_t)B->count * f;
   if ((rc = dalloc(&B->d_graw, ni)) || (rc = dalloc(&B->d_gcur, ni)) || (rc = dalloc(&B->d_gprev, ni)) ||
       (rc = dalloc(&B->d_wprev, ni)) || (rc = dalloc(&B->d_hdx, ni * depth)) ||
       (rc = dalloc(&B->d_hdg, ni * depth)) || (rc = dalloc(&B->d_gram, c * depth * depth)) ||
@@ -495,6 +521,32 @@ static int ensure_mix(scft_batch *B, int depth) {
   CK(host_alloc((void **)&B->h_nactive, sizeof(int)));
   B->depth = depth;
   return SCFT_OK;
+}
+
+// Copies the winning forked path of every instance into the instance's own
+// slots (field, density, Q, error, iterations, status); win[i] = iterations * 16
+// + path of the winner, INT_MAX when no path converged.
+__global__ void resolve_forks_kernel(int count, const int *n, const long long *node_off, long long rep_nodes,
+                                     const int *win, double *w, double *phi, double *Q, double *err, int *iters,
+                                     int *status, int *active) {
+  const int i = blockIdx.x;
+  const int key = win[i];
+  if (key == 0x7fffffff) return;
+  const int r = key & 15;
+  if (r == 0) return;
+  const int v = r * count + i;
+  const long long o = node_off[i], ro = o + r * rep_nodes;
+  for (int j = threadIdx.x; j < n[i]; j += blockDim.x) {
+    w[o + j] = w[ro + j];
+    phi[o + j] = phi[ro + j];
+  }
+  if (threadIdx.x == 0) {
+    Q[i] = Q[v];
+    err[i] = err[v];
+    iters[i] = iters[v];
+    status[i] = status[v] | ST_FORKED;
+    active[i] = 0;
+  }
 }
 
 static void destroy_batch(scft_batch *B) {
@@ -509,6 +561,10 @@ static void destroy_batch(scft_batch *B) {
   dfree(B->d_ds); dfree(B->d_x); dfree(B->d_f0); dfree(B->d_w); dfree(B->d_phi);
   dfree(B->d_Q); dfree(B->d_qw); dfree(B->d_node_off); dfree(B->d_int_off); dfree(B->d_heads);
   dfree(B->d_w0);
+  dfree(B->d_win);
+  dfree(B->d_fork);
+  if (B->h_fork) host_free(B->h_fork);
+  B->h_fork = nullptr;
   if (B->t0) cudaEventDestroy(B->t0);
   if (B->t1) cudaEventDestroy(B->t1);
   for (auto s : B->side) cudaStreamDestroy(s);
@@ -694,6 +750,7 @@ static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool veri
   CK(cudaMemsetAsync(B->d_ref_it, 0, c * sizeof(int), st));
 
   MixDev &m = *mp;
+  m = MixDev();  // no forks unless the fused solve sets them
   m.count = c;
   m.n = B->d_n;
   m.node_off = B->d_node_off;
@@ -755,7 +812,31 @@ static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
   const size_t live_bytes = (size_t)2 * B->live_maxc * sizeof(unsigned long long);
   CK(cudaMemsetAsync(B->d_work, 0, live_bytes, st));
   for (auto &c : plans) CK(cudaMemsetAsync(B->d_heads + c.head, 0, sizeof(int), st));
-  const BatchDev b = batch_dev(B);
+  BatchDev b = batch_dev(B);
+  const int nf = (o->finish_stall > 0) ? 0 : o->forks;  // forks and the FP64 hand-off exclude each other
+  std::vector<size_t> fork_off(plans.size(), 0);
+  if (nf > 0) {
+    m.base = B->count; m.rep_nodes = B->total_nodes; m.rep_int = B->total_int;
+    m.forks = nf; m.fork_at = o->fork_at; m.fork_grace = o->fork_grace; m.win = B->d_win;
+    for (int f = 0; f < 4; f++) m.fork_scale[f] = (f < nf) ? o->fork_scale[f] : 1.0;
+    b.base = B->count; b.rep_nodes = B->total_nodes;
+    if ((rc = fill_int(B->d_win, B->count, 0x7fffffff, st))) return rc;
+    // per class: {published, claimed, may still fork, unused} and one entry per instance
+    size_t need = 0;
+    for (size_t i = 0; i < plans.size(); i++) { fork_off[i] = need; need += 4 + plans[i].items.size(); }
+    if (need > B->fork_cap) {
+      dfree(B->d_fork);
+      if (B->h_fork) host_free(B->h_fork);
+      B->h_fork = nullptr;
+      B->fork_cap = 0;
+      if ((rc = dalloc(&B->d_fork, need))) return rc;
+      CK(host_alloc((void **)&B->h_fork, need * sizeof(int)));
+      B->fork_cap = need;
+    }
+    std::fill(B->h_fork, B->h_fork + need, 0);
+    for (size_t i = 0; i < plans.size(); i++) B->h_fork[fork_off[i] + 2] = (int)plans[i].items.size();
+    CK(cudaMemcpyAsync(B->d_fork, B->h_fork, need * sizeof(int), cudaMemcpyHostToDevice, st));
+  }
   B->pending_start = std::chrono::steady_clock::now();
   CK(cudaEventRecord(B->ev_fork, st));
   for (size_t i = 0; i < plans.size(); i++) {
@@ -766,6 +847,10 @@ static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
     class_dev(B, c, &d);
     const int li = live_index(B, 0, p, (int)i);
     d.work = B->d_work + li;
+    if (nf > 0) {
+      d.fork_ctl = B->d_fork + fork_off[i];
+      d.fork_list = d.fork_ctl + 4;
+    }
     // keep the class's share resident if the fused kernel fits fewer CTAs per SM
     // than the plan assumed
     int grid = c.grid;
@@ -781,6 +866,13 @@ static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
     CK(cudaEventRecord(B->ev_join[i], s));
   }
   for (size_t i = 0; i < plans.size(); i++) CK(cudaStreamWaitEvent(st, B->ev_join[i], 0));
+  if (nf > 0) {
+    resolve_forks_kernel<<<B->count, 128, 0, st>>>(B->count, B->d_n, B->d_node_off, B->total_nodes, B->d_win,
+                                                    B->d_w, B->d_phi, B->d_Q, B->d_err, B->d_iters,
+                                                    B->d_status, B->d_active);
+    g_launches++;
+    CK(cudaGetLastError());
+  }
   CK(cudaMemcpyAsync(B->h_work, B->d_work, live_bytes, cudaMemcpyDeviceToHost, st));
   count_active_kernel<<<1, 256, 0, st>>>(B->d_active, B->count, B->d_nactive);
   g_launches++;
@@ -901,6 +993,15 @@ static int check_opts(const scft_solve_opts *o) {
   if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
       !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0 || !(o->budget_ms >= 0.0))
     return set_err(SCFT_EINVAL, "solve options");
+  if (o->forks < 0 || o->forks > SCFT_MAX_FORKS)
+    return set_err(SCFT_EINVAL, "solve options: forks must be in [0, %d]", SCFT_MAX_FORKS);
+  if (o->forks > 0) {
+    if (o->fork_at < 1 || o->fork_grace < 0 || o->maxit > (1 << 26))
+      return set_err(SCFT_EINVAL, "solve options: forks need fork_at >= 1 and fork_grace >= 0");
+    for (int f = 0; f < o->forks; f++)
+      if (!(o->fork_scale[f] > 0.0 && o->fork_scale[f] * o->beta <= 1.0))
+        return set_err(SCFT_EINVAL, "solve options: fork_scale[%d] must give a mixing parameter in (0, 1]", f);
+  }
   return SCFT_OK;
 }
 
@@ -912,8 +1013,9 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   if (rc) return rc;
   const bool verify = (p == PREC_F32) && o->verify64;
   const bool need64 = (p == PREC_F64) || verify || o->finish_stall > 0;
-  if ((rc = ensure_mix(B, o->depth))) return rc;
-  if (o->fused && p == PREC_F32 && !verify) return solve_fused(B, o, res);
+  const bool fused = o->fused && p == PREC_F32 && !verify;
+  if ((rc = ensure_mix(B, o->depth, fused ? o->forks : 0))) return rc;
+  if (fused) return solve_fused(B, o, res);
   if (p == PREC_F32 && need64 && (rc = plan(B, PREC_F64, 0.125))) return rc;
   cudaStream_t st = B->st;
   CK(cudaEventRecord(B->t0, st));
@@ -1589,6 +1691,13 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->finish_stall = 0;
   o->finish_tol = 1e-4;
   o->budget_ms = 0.0;
+  o->forks = 3;
+  o->fork_at = 20;
+  o->fork_grace = 14;
+  o->fork_scale[0] = 0.9;
+  o->fork_scale[1] = 0.8;
+  o->fork_scale[2] = 0.6;
+  o->fork_scale[3] = 0.95;
 }
 
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {
@@ -1636,7 +1745,7 @@ int scft_batch_solve_async(scft_batch *b, const scft_solve_opts *opts) {
     return set_err(SCFT_EINVAL, "asynchronous solves run the fused FP32 form (fused = 1, verify64 = 0)");
   if (b->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
   int rc;
-  if ((rc = plan(b, PREC_F32, 1.0)) || (rc = ensure_mix(b, o->depth))) return rc;
+  if ((rc = plan(b, PREC_F32, 1.0)) || (rc = ensure_mix(b, o->depth, o->forks))) return rc;
   return solve_fused_enqueue(b, o);
 }
 
