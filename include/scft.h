@@ -184,6 +184,8 @@ typedef struct scft_solve_opts {
                          0: off.  Not used with finish_stall > 0 */
   int fork_at;
   int fork_grace;
+  int fork_first;     /* 1: thread groups take published forked paths before new instances; 0: only
+                         once the class's instances have all been taken */
   double fork_scale[4];
 } scft_solve_opts;
 

@@ -61,7 +61,7 @@ class ScftSolveOpts(C.Structure):
                 ("beta_schedule", C.c_int), ("weighted", C.c_int), ("step_cap", C.c_double),
                 ("field_floor", C.c_double), ("fused", C.c_int),
                 ("finish_stall", C.c_int), ("finish_tol", C.c_double), ("budget_ms", C.c_double),
-                ("forks", C.c_int), ("fork_at", C.c_int), ("fork_grace", C.c_int),
+                ("forks", C.c_int), ("fork_at", C.c_int), ("fork_grace", C.c_int), ("fork_first", C.c_int),
                 ("fork_scale", C.c_double * 4)]
 
 

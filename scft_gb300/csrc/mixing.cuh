@@ -56,6 +56,7 @@ struct MixDev {
   int base = 0;
   long long rep_nodes = 0, rep_int = 0;
   int forks = 0, fork_at = 0, fork_grace = 0;
+  int fork_first = 0;  // groups take published path jobs before new instances
   double fork_scale[4] = {1.0, 1.0, 1.0, 1.0};
   int *win = nullptr;
 };

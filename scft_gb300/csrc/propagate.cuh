@@ -145,12 +145,13 @@ struct Propagator {
   //
   // Forked paths (m.forks > 0): an instance that takes its update number
   // m.fork_at copies its state into m.forks further paths (mix_step) and
-  // publishes them here; once the class queue is empty, groups claim path jobs
-  // in publication order and iterate them the same way.  A job claimed before
-  // its fork is published is waited for (bounded: it ends when every instance
-  // of the class has forked or finished, at the time budget, or after
-  // FORK_WAIT_NS); the instances the waiting groups depend on are all held by
-  // running groups, which wait for nothing.
+  // publishes them here; groups claim published path jobs in publication order
+  // (before each instance of the class queue with m.fork_first, else once the
+  // queue is empty) and iterate them the same way.  Groups with nothing to
+  // claim wait until every instance of the class has forked or finished
+  // (bounded by the time budget and FORK_WAIT_NS of idle waiting); the
+  // instances they wait for are all held by running groups, which wait for
+  // nothing.
   __device__ static void solve(const BatchDev &b, const ClassDev &cls, const MixDev &m, GroupSmem<R, NW> &S,
                                MixSmem<NW> &MS, int P, int worker, int bar_id) {
     const int lane = P & 31, wid = P >> 5;
@@ -186,7 +187,31 @@ struct Propagator {
         }
       }
     };
+    // Claims the next published path job (thread 0 only): -1 when none is
+    // published and unclaimed.  A job is never claimed before its fork is
+    // counted; the fork's entry follows its count within a few instructions.
+    auto claim = [&]() -> int {
+      int h = *(volatile const int *)(cls.fork_ctl + 1);
+      for (int tries = 0; tries < 64; tries++) {
+        if (h >= *(volatile const int *)cls.fork_ctl * m.forks) return -1;
+        const int old = atomicCAS(cls.fork_ctl + 1, h, h + 1);
+        if (old == h) {
+          const int k = h / m.forks, f = h - k * m.forks;
+          int e = 0;
+          for (int s = 0; s < (1 << 20) && (e = *(volatile const int *)(cls.fork_list + k)) == 0; s++)
+            __nanosleep(100);
+          __threadfence();
+          return e ? (f + 1) * b.base + (e - 1) : -1;
+        }
+        h = old;
+      }
+      return -1;
+    };
     for (;;) {
+      if (forking && m.fork_first) {
+        const int v = bcast(P == 0 ? claim() : -1);
+        if (v >= 0) { run_path(v); continue; }
+      }
       const int item = bcast(P == 0 ? atomicAdd(cls.head, 1) : 0);
       if (item >= cls.count) break;
       const int inst = cls.items[item];
@@ -195,27 +220,27 @@ struct Propagator {
       if (forking && P == 0 && m.iters[inst] < m.fork_at) atomicSub(cls.fork_ctl + 2, 1);
     }
     if (!forking) return;
+    // the class queue is empty: path jobs until every instance has forked or
+    // finished and every published job is claimed
+    unsigned long long t0 = (P == 0) ? global_ns() : 0ull;
     for (;;) {
       int v = -1;
       if (P == 0) {
-        const int job = atomicAdd(cls.fork_ctl + 1, 1);
-        const int k = job / m.forks, f = job - k * m.forks;
-        if (k < cls.count) {
-          const unsigned long long t0 = global_ns();
-          for (;;) {
-            const int e = *(volatile const int *)(cls.fork_list + k);
-            if (e) { v = (f + 1) * b.base + (e - 1); break; }
-            if (*(volatile const int *)(cls.fork_ctl + 2) <= 0 && k >= *(volatile const int *)cls.fork_ctl) break;
-            const unsigned long long t = global_ns();
-            if ((m.deadline && t > __ldcg(m.deadline)) || t - t0 > FORK_WAIT_NS) break;
-            __nanosleep(4000);
-          }
-          __threadfence();
+        v = claim();
+        if (v < 0) {
+          const bool none_left = *(volatile const int *)(cls.fork_ctl + 2) <= 0 &&
+                                 *(volatile const int *)(cls.fork_ctl + 1) >= *(volatile const int *)cls.fork_ctl * m.forks;
+          const unsigned long long t = global_ns();
+          if (none_left || (m.deadline && t > __ldcg(m.deadline)) || t - t0 > FORK_WAIT_NS) v = -2;
+          else __nanosleep(4000);
         }
       }
       v = bcast(v);
-      if (v < 0) break;
-      run_path(v);
+      if (v == -2) break;
+      if (v >= 0) {
+        run_path(v);
+        if (P == 0) t0 = global_ns();
+      }
     }
   }
 

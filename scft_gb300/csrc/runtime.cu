@@ -817,7 +817,8 @@ static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
   std::vector<size_t> fork_off(plans.size(), 0);
   if (nf > 0) {
     m.base = B->count; m.rep_nodes = B->total_nodes; m.rep_int = B->total_int;
-    m.forks = nf; m.fork_at = o->fork_at; m.fork_grace = o->fork_grace; m.win = B->d_win;
+    m.forks = nf; m.fork_at = o->fork_at; m.fork_grace = o->fork_grace; m.fork_first = o->fork_first;
+    m.win = B->d_win;
     for (int f = 0; f < 4; f++) m.fork_scale[f] = (f < nf) ? o->fork_scale[f] : 1.0;
     b.base = B->count; b.rep_nodes = B->total_nodes;
     if ((rc = fill_int(B->d_win, B->count, 0x7fffffff, st))) return rc;
@@ -1692,8 +1693,9 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->finish_tol = 1e-4;
   o->budget_ms = 0.0;
   o->forks = 3;
-  o->fork_at = 20;
-  o->fork_grace = 14;
+  o->fork_at = 28;
+  o->fork_grace = 10;
+  o->fork_first = 1;
   o->fork_scale[0] = 0.9;
   o->fork_scale[1] = 0.8;
   o->fork_scale[2] = 0.6;

@@ -48,17 +48,20 @@ def test_forks_never_cost_iterations_and_keep_the_instances_own_wins():
 
 
 def test_forked_solve_does_not_depend_on_scheduling():
-    """Two synchronous solves and one asynchronous solve (next to another batch
-    in flight, so different groups take the paths) give identical results."""
+    """Synchronous solves with paths taken late or first, and an asynchronous
+    solve next to another batch in flight (so different groups take the paths),
+    give identical results."""
     insts = W.batch_mixed(96, seed=96)
     other = W.batch_mixed(64, seed=97)
     o = opts(forks=4, fork_at=5)
     runs = []
     with api.Batch(insts) as b, api.Batch(other) as c:
-        for k in range(3):
+        for k in range(4):
             b.reset()
             if k < 2:
                 r = b.solve(o)
+            elif k == 3:
+                r = b.solve(opts(forks=4, fork_at=5, fork_first=1))
             else:
                 c.reset()
                 c.solve_async(opts(forks=2, fork_at=3))
