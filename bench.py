@@ -259,7 +259,10 @@ def ours_arm(args):
 
     insts, desc = make_workload(args.workload, args.count)
     mine = [insts[i] for i in shard(insts, rank, world)]
-    opts = api.solve_opts(precision=F32, tol=TOL)
+    # forked paths for the noise-driven tail of the warm-started batch (3 paths
+    # from update 28 at an error <= 1e-5); off for the cold start, whose slow
+    # instances are slow for other reasons
+    opts = api.solve_opts(precision=F32, tol=TOL, forks=0 if args.cold else 3)
     b = api.Batch(mine)
     if args.autotune:
         b.autotune(F32)
@@ -347,11 +350,12 @@ def ours_arm(args):
                    "start": ("learned warm start (conv net, weights " + os.path.relpath(args.weights, ROOT) + ")")
                    if ws is not None else "cold (w0 ~ U[-0.1, 0.1])",
                    "l2": "working set (half-contour stores of concurrent instances) larger than L2",
-                   "mixing": "Anderson depth 10, beta 1.0, ln-residual with (1 - 0.6 d2/dx2) preconditioner; "
-                             f"instances still running after {opts.fork_at} updates fork into {opts.forks} paths "
-                             f"(beta x {', '.join(str(opts.fork_scale[k]) for k in range(opts.forks))}), own path "
-                             f"kept if converged by update {opts.fork_at + opts.fork_grace}, else the path with "
-                             "the fewest iterations",
+                   "mixing": "Anderson depth 10, beta 1.0, ln-residual with (1 - 0.6 d2/dx2) preconditioner"
+                             + (f"; instances still running after {opts.fork_at} updates fork (at an error <= "
+                                f"{opts.fork_err:g}) into {opts.forks} paths (beta x "
+                                f"{', '.join(str(opts.fork_scale[k]) for k in range(opts.forks))}); the own path "
+                                f"wins if converged within {opts.fork_grace} updates of the fork, else the path "
+                                "with the fewest iterations" if opts.forks else ""),
                    "parallelism": f"replicas x{world}, batch split by cost"},
         "gpu_launches": launches,
         "iterations_mean": statistics.mean(iters),
@@ -600,7 +604,7 @@ def profile_solve(args):
     with api.Batch(insts) as b:
         for _ in range(2):
             ws.predict(b)
-            r = b.solve(api.solve_opts(precision=F32, tol=TOL))
+            r = b.solve(api.solve_opts(precision=F32, tol=TOL, forks=3))
         torch.cuda.synchronize()
         print(json.dumps({"profile_solve": args.workload, "instances": len(insts), "ms": b.last_ms(),
                           "iterations_mean": float(r["iterations"].mean()), "live": b.live_stats(F32)}))

@@ -173,12 +173,13 @@ typedef struct scft_solve_opts {
   double budget_ms;   /* > 0: device-side time budget of the solve; a thread group that finds it
                          spent at an iteration boundary stops its instance with SCFT_ST_WATCHDOG
                          (the solve returns normally); 0: none */
-  int forks;          /* fused FP32 solves: an instance still running after fork_at iterations is
-                         copied into `forks` (<= SCFT_MAX_FORKS) further paths whose mixing parameter
-                         is beta times fork_scale[r]; thread groups that have run out of instances
-                         take these paths.  The instance's own path wins if it converges within
-                         fork_at + fork_grace iterations; otherwise the path that converges in the
-                         fewest iterations wins (ties: the lowest path, the instance itself first).
+  int forks;          /* fused FP32 solves: an instance still running after fork_at updates, at its
+                         first update taken with ||phi - f0||_inf <= fork_err, is copied into `forks`
+                         (<= SCFT_MAX_FORKS) further paths whose mixing parameter is beta times
+                         fork_scale[r]; idle thread groups take these paths.  The instance's own path
+                         wins if it converges within fork_grace updates of its fork; otherwise the
+                         path that converges in the fewest iterations wins (ties: the lowest path,
+                         the instance itself first).
                          The outcome does not depend on timing; paths stop once they cannot win.
                          The iteration count is the winner's, SCFT_ST_FORKED marks a forked winner.
                          0: off.  Not used with finish_stall > 0 */
@@ -186,6 +187,7 @@ typedef struct scft_solve_opts {
   int fork_grace;
   int fork_first;     /* 1: thread groups take published forked paths before new instances; 0: only
                          once the class's instances have all been taken */
+  double fork_err;
   double fork_scale[4];
 } scft_solve_opts;
 

@@ -35,6 +35,7 @@ struct scft_batch {
   std::vector<ClassPlan> plans[2];
   bool planned[2] = {false, false};
   double plan_frac[2] = {0, 0};
+  int plan_paths[2] = {0, 0};
   std::vector<int> shapeC[2], shapeNW[2];
   // Anderson state
   int depth = 0;
@@ -66,7 +67,7 @@ struct scft_batch {
   // state) hold 1 + paths copies; d_win per instance; d_fork the per-class fork
   // queues (4 control ints + one entry per instance), initialised from h_fork
   int paths = 0;
-  int *d_win = nullptr, *d_fork = nullptr, *h_fork = nullptr;
+  int *d_win = nullptr, *d_fork_it = nullptr, *d_fork = nullptr, *h_fork = nullptr;
   size_t fork_cap = 0;
   // a fused solve enqueued by scft_batch_solve_async, completed by scft_batch_wait
   bool pending = false;

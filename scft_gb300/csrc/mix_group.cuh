@@ -83,10 +83,15 @@ __device__ __forceinline__ double group_max(double v, MixSmem<NW> &S, int tid, S
   return warp_max(r);
 }
 
-// Key of path r converging after `it` updates (see MixDev::win): the instance's
-// own path (r = 0) within the grace iterations after the fork beats every path.
-__device__ __forceinline__ int fork_key(const MixDev &m, int it, int r) {
-  return (r == 0 && it <= m.fork_at + m.fork_grace) ? 0 : it * 16 + r;
+// Key of path r of instance ii converging after `it` updates (see
+// MixDev::win): the instance's own path (r = 0) before its fork or within the
+// grace updates after it beats every path.
+__device__ __forceinline__ int fork_key(const MixDev &m, int ii, int it, int r) {
+  if (r == 0) {
+    const int fit = m.fork_it[ii];
+    if (fit == 0 || it <= fit + m.fork_grace) return 0;
+  }
+  return it * 16 + r;
 }
 
 // One Anderson iteration of instance `inst` by threads tid = 0 .. 32*NW-1 of a
@@ -141,7 +146,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
       else {
         m.status[inst] |= ST_CONVERGED;
         m.active[inst] = 0;
-        if (m.win) atomicMin(m.win + ii, fork_key(m, it, r));
+        if (m.win) atomicMin(m.win + ii, fork_key(m, ii, it, r));
       }
     }
     return true;
@@ -157,7 +162,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     if (tid == 0) {
       int stop = 0;
       if (m.deadline && global_ns() > __ldcg(m.deadline)) stop = 1;
-      else if (m.win && fork_key(m, it + 1, r) > *(volatile const int *)(m.win + ii)) stop = 2;
+      else if (m.win && fork_key(m, ii, it + 1, r) > *(volatile const int *)(m.win + ii)) stop = 2;
       S.stop = stop;
     }
     sync();
@@ -270,10 +275,12 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
   //    step_cap / ds; the field is kept >= -field_floor / ds.
   const double beta = 1.0 - m.lk[inst];
   const double dsi = m.ds[ii];
-  // forked paths of this update (instance paths only, at update number fork_at):
-  // path f + 1 steps by d + beta (fork_scale[f] - 1) p, p the preconditioned
-  // residual, i.e. with its own mixing parameter; staged in its own wprev
-  const int nf = (m.forks > 0 && r == 0 && it + 1 == m.fork_at) ? min(m.forks, 4) : 0;
+  // forked paths of this update (an instance's own path forks once, at its
+  // first update number >= fork_at taken at an error <= fork_err): path f + 1
+  // steps by d + beta (fork_scale[f] - 1) p, p the preconditioned residual, i.e.
+  // with its own mixing parameter; staged in its own wprev
+  const int nf = (m.forks > 0 && r == 0 && it + 1 >= m.fork_at && e <= m.fork_err && m.fork_it[ii] == 0)
+                     ? min(m.forks, 4) : 0;
   double dm = 0.0, da = 0.0, dmf[4] = {0.0, 0.0, 0.0, 0.0}, daf[4] = {0.0, 0.0, 0.0, 0.0};
   for (int j = tid; j < N; j += NT) {
     const double gc = gcur[j];
@@ -373,6 +380,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
       m.lk[inst] = l;
     }
     S.forked = nf;
+    if (nf) m.fork_it[ii] = it + 1;
   }
   sync();
   return false;

@@ -47,16 +47,20 @@ struct MixDev {
   // Forked paths (BatchDev::base): static data at instance i, the node arrays
   // of path r at node_off[i] + r * rep_nodes, the interior arrays at
   // int_off[i] + r * rep_int (history: depth times that), scalars and the Gram
-  // matrix at id v.  forks > 0: an instance (r = 0) whose update number fork_at
-  // is taken copies its state into paths 1..forks, path r stepping with
-  // fork_scale[r - 1] times the step (and mixing parameter) of the instance.
+  // matrix at id v.  forks > 0: an instance (r = 0) copies its state into paths
+  // 1..forks when it forks, path r stepping with fork_scale[r - 1] times the
+  // mixing parameter of the instance.
+  // An instance forks at its first update number >= fork_at taken at an error
+  // <= fork_err; fork_it[i] records that update number (0: not forked).
   // win[i] = min over converged paths of their key, iterations * 16 + r, or 0
-  // for the instance's own path converging within fork_at + fork_grace
-  // iterations; a path stops once its earliest possible key exceeds win[i].
+  // for the instance's own path converging within fork_grace updates of its
+  // fork; a path stops once its earliest possible key exceeds win[i].
   int base = 0;
   long long rep_nodes = 0, rep_int = 0;
   int forks = 0, fork_at = 0, fork_grace = 0;
+  double fork_err = 0.0;
   int fork_first = 0;  // groups take published path jobs before new instances
+  int *fork_it = nullptr;
   double fork_scale[4] = {1.0, 1.0, 1.0, 1.0};
   int *win = nullptr;
 };

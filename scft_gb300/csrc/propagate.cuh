@@ -172,7 +172,7 @@ struct Propagator {
     auto run_path = [&](int v) {
       const int r = path_of(v, b.base), ii = v - r * b.base;
       // a forked path that can no longer win is not evaluated at all
-      if (r > 0 && bcast(P == 0 && fork_key(m, m.iters[v], r) > *(volatile const int *)(m.win + ii))) return;
+      if (r > 0 && bcast(P == 0 && fork_key(m, ii, m.iters[v], r) > *(volatile const int *)(m.win + ii))) return;
       for (;;) {
         instance(b, S, P, lane, wid, v, slot, bar_id);
         if (cls.work && P == 0)
@@ -216,8 +216,8 @@ struct Propagator {
       if (item >= cls.count) break;
       const int inst = cls.items[item];
       if (b.active[inst] == cls.want) run_path(inst);
-      // an instance that ends before its fork update never forks
-      if (forking && P == 0 && m.iters[inst] < m.fork_at) atomicSub(cls.fork_ctl + 2, 1);
+      // an instance that ends without forking never forks
+      if (forking && P == 0 && m.fork_it[inst] == 0) atomicSub(cls.fork_ctl + 2, 1);
     }
     if (!forking) return;
     // the class queue is empty: path jobs until every instance has forked or

@@ -264,9 +264,11 @@ static int ensure_streams(scft_batch *B, int nside) {
   return SCFT_OK;
 }
 
-// Plan the shape classes of precision p with `frac` of the GPU's resident CTAs.
-static int plan(scft_batch *B, int p, double frac) {
-  if (B->planned[p] && B->plan_frac[p] == frac) return SCFT_OK;
+// Plan the shape classes of precision p with `frac` of the GPU's resident CTAs;
+// `paths` forked paths per instance may add thread groups to a class beyond one
+// per instance (a class of few instances then runs its forks side by side).
+static int plan(scft_batch *B, int p, double frac, int paths = 0) {
+  if (B->planned[p] && B->plan_frac[p] == frac && B->plan_paths[p] == paths) return SCFT_OK;
   free_plans(B, p);
   const int sms = device_sms();
   if (sms <= 0) return set_err(SCFT_ENODEV, "no CUDA device");
@@ -303,7 +305,7 @@ static int plan(scft_batch *B, int p, double frac) {
     c.gpc = propagate_groups_per_cta(c.C, c.NW);
     int budget = (int)std::floor(cost / total * frac * cps * sms + 0.5);
     budget = std::max(1, budget);
-    c.workers = std::min((int)c.items.size(), budget * c.gpc);
+    c.workers = (int)std::min((long long)c.items.size() * (1 + paths), (long long)budget * c.gpc);
     c.grid = (c.workers + c.gpc - 1) / c.gpc;
     c.slot_elems = (long long)(maxhalf + 1) * 32 * c.NW * c.C;
     const size_t esz = (p == PREC_F32) ? 4 : 8;
@@ -333,6 +335,7 @@ static int plan(scft_batch *B, int p, double frac) {
   }
   B->planned[p] = true;
   B->plan_frac[p] = frac;
+  B->plan_paths[p] = paths;
   return ensure_streams(B, (int)std::max(B->plans[0].size(), B->plans[1].size()));
 }
 
@@ -505,7 +508,8 @@ static int ensure_mix(scft_batch *B, int depth, int paths = 0) {
         (rc = grow_array(B->d_active, c * f0, c * f1)))
       return rc;
     dfree(B->d_win);
-    if ((rc = dalloc(&B->d_win, c))) return rc;
+    dfree(B->d_fork_it);
+    if ((rc = dalloc(&B->d_win, c)) || (rc = dalloc(&B->d_fork_it, c))) return rc;
   }
   free_mix(B);
   B->paths = paths;
@@ -562,6 +566,7 @@ static void destroy_batch(scft_batch *B) {
   dfree(B->d_Q); dfree(B->d_qw); dfree(B->d_node_off); dfree(B->d_int_off); dfree(B->d_heads);
   dfree(B->d_w0);
   dfree(B->d_win);
+  dfree(B->d_fork_it);
   dfree(B->d_fork);
   if (B->h_fork) host_free(B->h_fork);
   B->h_fork = nullptr;
@@ -818,7 +823,8 @@ static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
   if (nf > 0) {
     m.base = B->count; m.rep_nodes = B->total_nodes; m.rep_int = B->total_int;
     m.forks = nf; m.fork_at = o->fork_at; m.fork_grace = o->fork_grace; m.fork_first = o->fork_first;
-    m.win = B->d_win;
+    m.fork_err = o->fork_err; m.win = B->d_win; m.fork_it = B->d_fork_it;
+    CK(cudaMemsetAsync(B->d_fork_it, 0, B->count * sizeof(int), st));
     for (int f = 0; f < 4; f++) m.fork_scale[f] = (f < nf) ? o->fork_scale[f] : 1.0;
     b.base = B->count; b.rep_nodes = B->total_nodes;
     if ((rc = fill_int(B->d_win, B->count, 0x7fffffff, st))) return rc;
@@ -997,8 +1003,8 @@ static int check_opts(const scft_solve_opts *o) {
   if (o->forks < 0 || o->forks > SCFT_MAX_FORKS)
     return set_err(SCFT_EINVAL, "solve options: forks must be in [0, %d]", SCFT_MAX_FORKS);
   if (o->forks > 0) {
-    if (o->fork_at < 1 || o->fork_grace < 0 || o->maxit > (1 << 26))
-      return set_err(SCFT_EINVAL, "solve options: forks need fork_at >= 1 and fork_grace >= 0");
+    if (o->fork_at < 1 || o->fork_grace < 0 || !(o->fork_err > 0.0) || o->maxit > (1 << 26))
+      return set_err(SCFT_EINVAL, "solve options: forks need fork_at >= 1, fork_grace >= 0, fork_err > 0");
     for (int f = 0; f < o->forks; f++)
       if (!(o->fork_scale[f] > 0.0 && o->fork_scale[f] * o->beta <= 1.0))
         return set_err(SCFT_EINVAL, "solve options: fork_scale[%d] must give a mixing parameter in (0, 1]", f);
@@ -1010,11 +1016,11 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   const int p = o->precision;
   if (check_opts(o)) return SCFT_EINVAL;
   if (B->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
-  int rc = plan(B, p, 1.0);
-  if (rc) return rc;
   const bool verify = (p == PREC_F32) && o->verify64;
   const bool need64 = (p == PREC_F64) || verify || o->finish_stall > 0;
   const bool fused = o->fused && p == PREC_F32 && !verify;
+  int rc = plan(B, p, 1.0, (fused && o->finish_stall == 0) ? o->forks : 0);
+  if (rc) return rc;
   if ((rc = ensure_mix(B, o->depth, fused ? o->forks : 0))) return rc;
   if (fused) return solve_fused(B, o, res);
   if (p == PREC_F32 && need64 && (rc = plan(B, PREC_F64, 0.125))) return rc;
@@ -1692,10 +1698,11 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->finish_stall = 0;
   o->finish_tol = 1e-4;
   o->budget_ms = 0.0;
-  o->forks = 3;
+  o->forks = 0;
   o->fork_at = 28;
   o->fork_grace = 10;
   o->fork_first = 1;
+  o->fork_err = 1e-5;
   o->fork_scale[0] = 0.9;
   o->fork_scale[1] = 0.8;
   o->fork_scale[2] = 0.6;
@@ -1747,7 +1754,8 @@ int scft_batch_solve_async(scft_batch *b, const scft_solve_opts *opts) {
     return set_err(SCFT_EINVAL, "asynchronous solves run the fused FP32 form (fused = 1, verify64 = 0)");
   if (b->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
   int rc;
-  if ((rc = plan(b, PREC_F32, 1.0)) || (rc = ensure_mix(b, o->depth, o->forks))) return rc;
+  if ((rc = plan(b, PREC_F32, 1.0, o->finish_stall == 0 ? o->forks : 0)) || (rc = ensure_mix(b, o->depth, o->forks)))
+    return rc;
   return solve_fused_enqueue(b, o);
 }
 

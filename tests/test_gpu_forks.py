@@ -88,7 +88,7 @@ def test_fork_options_are_checked():
     insts = W.batch_mixed(4, seed=98)
     with api.Batch(insts) as b:
         for bad in (dict(forks=5), dict(forks=-1), dict(forks=2, fork_at=0),
-                    dict(forks=2, fork_grace=-1)):
+                    dict(forks=2, fork_grace=-1), dict(forks=2, fork_err=0.0)):
             with pytest.raises(ScftError):
                 b.solve(opts(**bad))
         o = opts(forks=1, beta=1.0)
