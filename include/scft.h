@@ -189,6 +189,13 @@ typedef struct scft_solve_opts {
                          once the class's instances have all been taken */
   double fork_err;
   double fork_scale[4];
+  double graded_ratio;   /* instances whose mesh has largest / smallest element above this ratio (0:
+                            none) take the graded-mesh step: preconditioner spacings floored at
+                            sqrt(precond_hfloor * ds), the contour diffusion scale below which the
+                            preconditioner's curvature means nothing, and each node's move clamped
+                            to step_cap / ds instead of the whole step scaled (one wall node of a
+                            mesh graded to 1e-6 would otherwise throttle every other node) */
+  double precond_hfloor;
 } scft_solve_opts;
 
 typedef struct scft_result {

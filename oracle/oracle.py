@@ -63,12 +63,12 @@ class MixOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("beta", C.c_double), ("clip", C.c_double), ("grow", C.c_double),
                 ("reg", C.c_double), ("precond", C.c_double), ("maxit", C.c_int), ("depth", C.c_int),
                 ("mode", C.c_int), ("schedule", C.c_int), ("cap", C.c_double), ("floor", C.c_double),
-                ("weighted", C.c_int)]
+                ("weighted", C.c_int), ("graded_ratio", C.c_double), ("hfloor", C.c_double)]
 
 
 # the batched GPU solver's defaults (scft_solve_opts_init)
 MIX_DEFAULTS = dict(tol=1e-6, beta=1.0, clip=1.0, grow=10.0, reg=1e-12, precond=0.6, maxit=2000,
-                    depth=10, mode=1, schedule=0, cap=0.25, floor=0.5, weighted=1)
+                    depth=10, mode=1, schedule=0, cap=0.25, floor=0.5, weighted=1, graded_ratio=16.0, hfloor=0.1)
 
 
 def _ptr(a: np.ndarray):

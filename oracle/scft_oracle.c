@@ -1004,6 +1004,13 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
   for (int j = 0; j < N; j++) fmx = fmax(fmx, p->f0[j + 1]);
   const double winv = (o->weighted && fmx > 0.0) ? 1.0 / fmx : 0.0;
   const double wfloor = o->floor > 0.0 ? -o->floor / p->ds : -INFINITY;
+  double hmin = INFINITY, hmax = 0.0;
+  for (int k = 1; k < n; k++) {
+    hmin = fmin(hmin, p->x[k] - p->x[k - 1]);
+    hmax = fmax(hmax, p->x[k] - p->x[k - 1]);
+  }
+  const int graded = o->graded_ratio > 0.0 && hmax / hmin > o->graded_ratio;
+  const double hf = graded ? sqrt(o->hfloor * p->ds) : 0.0;
   w[0] = w[n - 1] = 0.0;
   for (it = 0;; it++) {
     if (or_propagate(p, w, phi, NULL, NULL)) { rc = -3; break; }
@@ -1064,7 +1071,7 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
     for (int j = 0; j < N; j++) {
       double gc = g[j], lap = 0.0;
       if (j > 0 && j < N - 1) {
-        double a1 = p->x[j + 1] - p->x[j], a2 = p->x[j + 2] - p->x[j + 1];
+        double a1 = fmax(p->x[j + 1] - p->x[j], hf), a2 = fmax(p->x[j + 2] - p->x[j + 1], hf);
         lap = ((gc - g[j - 1]) / a1 + (gc - g[j + 1]) / a2) / (0.5 * (a1 + a2));
       }
       double step = (1.0 - lk) * (gc + o->precond * lap);
@@ -1074,12 +1081,14 @@ int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int 
       da = fmax(da, fabs(step));
     }
     double scale = dm > o->clip ? o->clip / dm : 1.0;
-    if (o->cap > 0.0 && da * scale * p->ds > o->cap) scale = o->cap / (da * p->ds);
+    if (!graded && o->cap > 0.0 && da * scale * p->ds > o->cap) scale = o->cap / (da * p->ds);
+    const double lim = o->cap / p->ds;
     for (int j = 0; j < N; j++) {
-      double step = wprev[j];
+      double dw = scale * wprev[j];
+      if (graded && o->cap > 0.0) dw = fmin(fmax(dw, -lim), lim);
       wprev[j] = w[j + 1];
       gprev[j] = graw[j];
-      w[j + 1] = fmax(w[j + 1] + scale * step, wfloor);
+      w[j + 1] = fmax(w[j + 1] + dw, wfloor);
     }
     if (o->schedule) {
       if (e < 0.03 && it > 100) lk *= lmd;

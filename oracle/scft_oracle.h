@@ -110,6 +110,11 @@ typedef struct or_mix_opts {
   int maxit, depth, mode, schedule; /* schedule: beta = 1 - lk with lk of ADM_chen_C.c:125-129 */
   double cap, floor;                /* 0 disables either */
   int weighted;
+  /* meshes whose largest / smallest element exceeds graded_ratio (0: never)
+     take the graded-mesh step: preconditioner spacings floored at
+     sqrt(hfloor * ds), and each node's move clamped to cap / ds instead of the
+     whole step scaled */
+  double graded_ratio, hfloor;
 } or_mix_opts;
 int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int *iters, double *err);
 

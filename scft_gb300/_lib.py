@@ -63,7 +63,7 @@ class ScftSolveOpts(C.Structure):
                 ("finish_stall", C.c_int), ("finish_tol", C.c_double), ("budget_ms", C.c_double),
                 ("forks", C.c_int), ("fork_at", C.c_int), ("fork_grace", C.c_int), ("fork_first", C.c_int),
                 ("fork_err", C.c_double),
-                ("fork_scale", C.c_double * 4)]
+                ("fork_scale", C.c_double * 4), ("graded_ratio", C.c_double), ("precond_hfloor", C.c_double)]
 
 
 class ScftResult(C.Structure):

@@ -21,12 +21,13 @@ struct scft_batch {
   int count = 0;
   std::vector<int> n, nsteps, rule;
   std::vector<double> ds;
+  std::vector<double> spacing_ratio;  // largest / smallest element of each mesh
   std::vector<long long> node_off, int_off;
   long long total_nodes = 0, total_int = 0;
   // device instance data
   int *d_n = nullptr, *d_nsteps = nullptr, *d_active = nullptr, *d_status = nullptr;
   double *d_ds = nullptr, *d_x = nullptr, *d_f0 = nullptr, *d_w = nullptr, *d_phi = nullptr;
-  double *d_Q = nullptr, *d_qw = nullptr, *d_w0 = nullptr;
+  double *d_Q = nullptr, *d_qw = nullptr, *d_w0 = nullptr, *d_spacing = nullptr;
   long long *d_node_off = nullptr, *d_int_off = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   float last_ms = 0.f;

@@ -275,6 +275,8 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
   //    step_cap / ds; the field is kept >= -field_floor / ds.
   const double beta = 1.0 - m.lk[inst];
   const double dsi = m.ds[ii];
+  const bool graded = m.spacing && m.graded_ratio > 0.0 && m.spacing[ii] > m.graded_ratio;
+  const double hf = graded ? sqrt(m.hfloor * dsi) : 0.0;  // preconditioner spacing floor
   // forked paths of this update (an instance's own path forks once, at its
   // first update number >= fork_at taken at an error <= fork_err): path f + 1
   // steps by d + beta (fork_scale[f] - 1) p, p the preconditioned residual, i.e.
@@ -286,7 +288,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     const double gc = gcur[j];
     double lap = 0.0;
     if (j > 0 && j < N - 1) {
-      const double a1 = x[j + 1] - x[j], a2 = x[j + 2] - x[j + 1];
+      const double a1 = fmax(x[j + 1] - x[j], hf), a2 = fmax(x[j + 2] - x[j + 1], hf);
       lap = ((gc - gcur[j - 1]) / a1 + (gc - gcur[j + 1]) / a2) / (0.5 * (a1 + a2));
     }
     const double pr = gc + m.precond * lap;
@@ -306,12 +308,15 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
       }
   }
   // the step is scaled so that its f0-weighted max norm is <= clip and no node
-  // moves by more than step_cap / ds
+  // moves by more than step_cap / ds (graded meshes: that bound clamps each
+  // node's move instead)
   auto step_scale = [&](double vm, double va) {
     double sc = (vm > m.clip) ? m.clip / vm : 1.0;
-    if (m.step_cap > 0.0 && va * sc * dsi > m.step_cap) sc = m.step_cap / (va * dsi);
+    if (!graded && m.step_cap > 0.0 && va * sc * dsi > m.step_cap) sc = m.step_cap / (va * dsi);
     return sc;
   };
+  const double lim = (graded && m.step_cap > 0.0) ? m.step_cap / dsi : INFINITY;
+  auto move = [&](double v) { return fmin(fmax(v, -lim), lim); };
   dm = group_max(dm, S, tid, sync);
   da = group_max(da, S, tid, sync);
   const double scale = step_scale(dm, da);
@@ -329,7 +334,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
     const double d = wprev[j];
     wprev[j] = wo;
     gprev[j] = graw[j];
-    w[j + 1] = fmax(wo + scale * d, wfloor);
+    w[j + 1] = fmax(wo + move(scale * d), wfloor);
 #pragma unroll
     for (int f = 0; f < 4; f++)
       if (f < nf) {
@@ -337,7 +342,7 @@ __device__ bool mix_step(const MixDev &m, int inst, int tid, MixSmem<NW> &S, Syn
         const double df = m.wprev[fo + j];
         m.wprev[fo + j] = wo;
         m.gprev[fo + j] = graw[j];
-        m.w[no + (f + 1) * m.rep_nodes + j + 1] = fmax(wo + scf[f] * df, wfloor);
+        m.w[no + (f + 1) * m.rep_nodes + j + 1] = fmax(wo + move(scf[f] * df), wfloor);
       }
   }
   if (nf) {

@@ -44,6 +44,11 @@ struct MixDev {
   // time budget: globaltimer (ns) after which a group stops its instance with
   // ST_WATCHDOG at the next iteration boundary; null: no budget
   const unsigned long long *deadline;
+  // graded meshes (spacing[i] = largest / smallest element > graded_ratio): the
+  // preconditioner's spacings are floored at sqrt(hfloor * ds) and each node's
+  // move is clamped to step_cap / ds instead of scaling the whole step
+  const double *spacing = nullptr;
+  double graded_ratio = 0.0, hfloor = 0.0;
   // Forked paths (BatchDev::base): static data at instance i, the node arrays
   // of path r at node_off[i] + r * rep_nodes, the interior arrays at
   // int_off[i] + r * rep_int (history: depth times that), scalars and the Gram

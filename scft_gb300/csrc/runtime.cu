@@ -565,6 +565,7 @@ static void destroy_batch(scft_batch *B) {
   dfree(B->d_ds); dfree(B->d_x); dfree(B->d_f0); dfree(B->d_w); dfree(B->d_phi);
   dfree(B->d_Q); dfree(B->d_qw); dfree(B->d_node_off); dfree(B->d_int_off); dfree(B->d_heads);
   dfree(B->d_w0);
+  dfree(B->d_spacing);
   dfree(B->d_win);
   dfree(B->d_fork_it);
   dfree(B->d_fork);
@@ -592,7 +593,7 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
   scft_batch *B = new scft_batch();
   B->count = count;
   B->n.resize(count); B->nsteps.resize(count); B->rule.resize(count); B->ds.resize(count);
-  B->node_off.resize(count); B->int_off.resize(count);
+  B->node_off.resize(count); B->int_off.resize(count); B->spacing_ratio.resize(count);
   for (int p = 0; p < 2; p++) { B->shapeC[p].assign(count, 0); B->shapeNW[p].assign(count, 0); }
   long long no = 0, io = 0;
   for (int i = 0; i < count; i++) {
@@ -607,13 +608,21 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
       destroy_batch(B);
       return set_err(SCFT_EINVAL, "instance %d: Romberg needs a power-of-two step count >= 16", i);
     }
+    double hmin = 1.0, hmax = 1.0;  // uniform when x is not given
     if (s.x) {
-      for (int k = 1; k < s.n_nodes; k++)
-        if (!(s.x[k] > s.x[k - 1])) {
+      hmin = INFINITY;
+      hmax = 0.0;
+      for (int k = 1; k < s.n_nodes; k++) {
+        const double h = s.x[k] - s.x[k - 1];
+        if (!(h > 0.0)) {
           destroy_batch(B);
           return set_err(SCFT_EINVAL, "instance %d: mesh not strictly increasing", i);
         }
+        hmin = std::min(hmin, h);
+        hmax = std::max(hmax, h);
+      }
     }
+    B->spacing_ratio[i] = hmax / hmin;
     B->n[i] = s.n_nodes; B->nsteps[i] = s.nsteps; B->rule[i] = s.rule; B->ds[i] = s.ds;
     B->node_off[i] = no; B->int_off[i] = io;
     no += s.n_nodes; io += s.n_nodes - 2;
@@ -625,7 +634,7 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
       (rc = dalloc(&B->d_f0, no)) || (rc = dalloc(&B->d_w, no)) || (rc = dalloc(&B->d_phi, no)) ||
       (rc = dalloc(&B->d_Q, count)) || (rc = dalloc(&B->d_qw, 16 * (size_t)count)) ||
       (rc = dalloc(&B->d_node_off, count)) || (rc = dalloc(&B->d_int_off, count)) ||
-      (rc = dalloc(&B->d_w0, no))) {
+      (rc = dalloc(&B->d_w0, no)) || (rc = dalloc(&B->d_spacing, count))) {
     destroy_batch(B);
     return rc;
   }
@@ -637,14 +646,14 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
   }
   // one pinned staging buffer (from the library's cache) for every upload
   const size_t nd = (size_t)no, nc = (size_t)count;
-  const size_t stage_doubles = 3 * nd + 16 * nc + nc + 2 * nc + nc;  // x, f0, w | qw | ds | offsets | n+nsteps
+  const size_t stage_doubles = 3 * nd + 16 * nc + 2 * nc + 2 * nc + nc;  // x, f0, w | qw | ds, spacing | offsets | n+nsteps
   double *stage = nullptr;
   if (host_alloc((void **)&stage, stage_doubles * sizeof(double)) != cudaSuccess) {
     destroy_batch(B);
     return set_err(SCFT_ENOMEM, "pinned staging buffer of %zu bytes", stage_doubles * sizeof(double));
   }
-  double *hx = stage, *hf = hx + nd, *hw = hf + nd, *hqw = hw + nd, *hds = hqw + 16 * nc;
-  long long *hno = reinterpret_cast<long long *>(hds + nc), *hio = hno + nc;
+  double *hx = stage, *hf = hx + nd, *hw = hf + nd, *hqw = hw + nd, *hds = hqw + 16 * nc, *hsp = hds + nc;
+  long long *hno = reinterpret_cast<long long *>(hsp + nc), *hio = hno + nc;
   int *hn = reinterpret_cast<int *>(hio + nc), *hns = hn + nc;
   for (int i = 0; i < count; i++) {
     const scft_instance &s = inst[i];
@@ -657,6 +666,7 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
     if (!s.x) hx[o + s.n_nodes - 1] = s.L;
     quad_table(s.nsteps, s.ds, s.rule, hqw + 16 * (size_t)i);
     hds[i] = s.ds;
+    hsp[i] = B->spacing_ratio[i];
     hno[i] = o;
     hio[i] = B->int_off[i];
     hn[i] = s.n_nodes;
@@ -667,6 +677,7 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
       {B->d_n, hn, nc * sizeof(int)},
       {B->d_nsteps, hns, nc * sizeof(int)},
       {B->d_ds, hds, nc * sizeof(double)},
+      {B->d_spacing, hsp, nc * sizeof(double)},
       {B->d_node_off, hno, nc * sizeof(long long)},
       {B->d_int_off, hio, nc * sizeof(long long)},
       {B->d_x, hx, nd * sizeof(double)},
@@ -773,6 +784,7 @@ static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool veri
   m.finish_stall = (p == PREC_F32) ? o->finish_stall : 0;
   m.finish_tol = o->finish_tol;
   m.ref_err = B->d_ref_err; m.ref_it = B->d_ref_it;
+  m.spacing = B->d_spacing; m.graded_ratio = o->graded_ratio; m.hfloor = o->precond_hfloor;
   m.deadline = nullptr;
   if (o->budget_ms > 0.0) {
     set_deadline_kernel<<<1, 1, 0, st>>>(B->d_deadline, (unsigned long long)(o->budget_ms * 1e6));
@@ -998,7 +1010,8 @@ static int graph_iterate(scft_batch *B, const scft_solve_opts *o, const MixDev &
 static int check_opts(const scft_solve_opts *o) {
   const int p = o->precision;
   if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
-      !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0 || !(o->budget_ms >= 0.0))
+      !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0 || !(o->budget_ms >= 0.0) ||
+      !(o->graded_ratio >= 0.0) || !(o->precond_hfloor >= 0.0))
     return set_err(SCFT_EINVAL, "solve options");
   if (o->forks < 0 || o->forks > SCFT_MAX_FORKS)
     return set_err(SCFT_EINVAL, "solve options: forks must be in [0, %d]", SCFT_MAX_FORKS);
@@ -1707,6 +1720,8 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->fork_scale[1] = 0.8;
   o->fork_scale[2] = 0.6;
   o->fork_scale[3] = 0.95;
+  o->graded_ratio = 16.0;
+  o->precond_hfloor = 0.1;
 }
 
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out) {
