@@ -168,7 +168,7 @@ typedef struct scft_solve_opts {
   int finish_stall;   /* FP32 solves: an instance whose error is below finish_tol and has not halved
                          for this many iterations continues with the FP64 propagator (fresh Anderson
                          history, tolerance tol, status bit SCFT_ST_FP64); 0: off.  FP32 rounding
-                         noise in the density (~1e-7) corrupts the secant pairs of small steps */
+                         in the density, amplified by the least squares, lengthens the tail */
   double finish_tol;
   double budget_ms;   /* > 0: device-side time budget of the solve; a thread group that finds it
                          spent at an iteration boundary stops its instance with SCFT_ST_WATCHDOG
