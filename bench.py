@@ -585,8 +585,8 @@ def config_legs(ws):
                                 "alg_GBps_fp32": alg / (ms32 / 1e3) / 1e9, "frac_of_peak": alg / (ms32 / 1e3) / 1e9 / peak,
                                 "peak_source": kind}
 
-    # the graded workload solved: 16 instances (one wave; each instance's chain of
-    # passes decides the time), graded-mesh step, FP32 stopping at the tolerance
+    # the graded workload solved: 16 instances (one wave of 4-CTA clusters; each
+    # instance's chain of passes decides the time), graded-mesh step, FP32 stopping at the tolerance
     # itself (these meshes leave a discretisation floor near 5e-7 on ||phi - f0||),
     # cold and learned starts, every field then checked under the FP64 propagator
     sub = insts[:16]
@@ -608,8 +608,9 @@ def config_legs(ws):
             solves[start] = {"ms": ms, "converged": conv, "value": conv / (ms / 1e3), "unit": UNIT,
                              "iterations_mean": float(r["iterations"].mean()), "iterations_max": int(r["iterations"].max()),
                              "fp64_verified": int(sum(e <= TOL for e in e64)), "fp64_err_max": max(e64)}
-    out["batch_graded_solve"] = {"workload": "16 instances of the graded workload, FP32 fused solve to 1e-6 "
-                                             "(FP32 stop at 1e-6), graded-mesh step, maxit 400",
+    out["batch_graded_solve"] = {"workload": "16 instances of the graded workload, FP32 solve to 1e-6 "
+                                             "(FP32 stop at 1e-6), graded-mesh step, maxit 400; batch-wide form "
+                                             "with the 4-CTA cluster propagator",
                                  "instances": len(sub), **solves}
     torch.cuda.synchronize()
     return out

@@ -164,7 +164,9 @@ typedef struct scft_solve_opts {
   int fused;          /* 1: each instance iterates on its own inside one persistent launch per shape
                          class (contour pass and Anderson step by the same thread group, no barrier
                          across the batch; FP32 without verify64); 0: every iteration is a batch-wide
-                         step (propagator launches, then the mixing kernel) replayed from CUDA graphs */
+                         step (propagator launches, then the mixing kernel) replayed from CUDA graphs.
+                         Batches with instances whose shape runs as a thread-block cluster (the default
+                         shapes above 2048 interior unknowns) take the batch-wide form */
   int finish_stall;   /* FP32 solves: an instance whose error is below finish_tol and has not halved
                          for this many iterations continues with the FP64 propagator (fresh Anderson
                          history, tolerance tol, status bit SCFT_ST_FP64); 0: off.  FP32 rounding

@@ -29,6 +29,13 @@ struct BatchDev {
   long long rep_nodes = 0;
 };
 
+// CTAs per thread-block cluster of the (precision, C, NW) propagator class: the
+// shapes that would spill registers at 32*NW threads in one CTA run as clusters
+// of 256-thread CTAs (see Propagator); 1 = one CTA per group.
+__host__ __device__ constexpr int cluster_ctas(bool f64, int C, int NW) {
+  return NW == 32 ? 4 : (NW == 16 && (C == 8 || (f64 && C == 4))) ? 2 : 1;
+}
+
 // Path and instance of id v (see BatchDev::base).
 __host__ __device__ __forceinline__ int path_of(int v, int base) { return base ? v / base : 0; }
 

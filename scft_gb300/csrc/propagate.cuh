@@ -29,6 +29,7 @@
 // Kahan-compensated.
 // FP64 path (DELTA = false): the direct form D q' = M q of the reference.
 #pragma once
+#include <cooperative_groups.h>
 #include <type_traits>
 
 #include "common.cuh"
@@ -97,18 +98,36 @@ struct Log2 { static constexpr int v = NW <= 1 ? 0 : 1 + Log2<NW / 2>::v; };
 template <>
 struct Log2<1> { static constexpr int v = 0; };
 
-template <typename R, int C, int NW, bool DELTA>
+// CL > 1: the group of one instance spans a thread-block cluster of CL CTAs of
+// 32*NW/CL threads each (large shapes, whose 32*NW threads would otherwise get
+// too few registers per thread in one CTA).  Group-level values are written to
+// the shared memory of every CTA of the cluster (distributed shared memory) and
+// read locally; the group barrier is the cluster barrier.
+template <typename R, int C, int NW, bool DELTA, int CL = 1>
 struct Propagator {
   static constexpr int T = 32 * NW;
   static constexpr int TC = T * C;
-  static constexpr int GPC = (T >= 64) ? 1 : 64 / T;    // groups per CTA (small CTAs: occupancy is register-bound)
-  static constexpr int CTA = T * GPC;
+  static constexpr int GPC = (CL > 1 || T >= 64) ? 1 : 64 / T;  // groups per CTA (small CTAs: occupancy is register-bound)
+  static constexpr int CTA = (CL > 1) ? T / CL : T * GPC;
+  static_assert(CL == 1 || (NW % CL == 0 && NW / CL >= 1), "cluster CTAs hold whole warps");
   static constexpr int L2 = Log2<NW>::v;
   static constexpr int CI = (C > 1) ? C - 1 : 1;       // chunk-interior array extent
 
   __device__ static void gsync(int bar_id) {
-    if (NW > 1) group_sync(bar_id, T);
+    if constexpr (CL > 1) cooperative_groups::this_cluster().sync();
+    else if (NW > 1) group_sync(bar_id, T);
     else __syncwarp();
+  }
+  // store a group-level value where every thread of the group reads it
+  template <typename V>
+  __device__ static __forceinline__ void put(V &ref, V v) {
+    if constexpr (CL > 1) {
+      cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+#pragma unroll
+      for (int r = 0; r < CL; r++) *cl.map_shared_rank(&ref, r) = v;
+    } else {
+      ref = v;
+    }
   }
 
   __device__ static void run(const BatchDev &b, const ClassDev &cls, GroupSmem<R, NW> &S,
@@ -118,7 +137,7 @@ struct Propagator {
     for (;;) {
       int item;
       if (NW > 1) {
-        if (P == 0) S.item = atomicAdd(cls.head, 1);
+        if (P == 0) put(S.item, atomicAdd(cls.head, 1));
         gsync(bar_id);
         item = S.item;
         gsync(bar_id);
@@ -160,7 +179,7 @@ struct Propagator {
     // value of thread 0 for the whole group
     auto bcast = [&](int v) -> int {
       if (NW > 1) {
-        if (P == 0) S.item = v;
+        if (P == 0) put(S.item, v);
         gsync(bar_id);
         v = S.item;
         gsync(bar_id);
@@ -444,7 +463,10 @@ struct Propagator {
     const long long off = b.node_off[ii], doff = off + path * b.rep_nodes;
     const double *x = b.x + off;
     const double *w = b.w + doff;
-    if (P < 16) S.qw[P] = (R)b.qw[(long long)ii * 16 + P];
+    {
+      const int loc = (CL > 1) ? (int)threadIdx.x : P;  // every CTA of a cluster keeps its own weights
+      if (loc < 16) S.qw[loc] = (R)b.qw[(long long)ii * 16 + loc];
+    }
     gsync(bar_id);
     int bad = 0;
 
@@ -523,7 +545,7 @@ struct Propagator {
     // next chunk's spikes at its first interior unknown (lane 31: from the next warp)
     double vcn = __shfl_down_sync(FULL, vc0, 1), wcn = __shfl_down_sync(FULL, wc0, 1);
     if (NW > 1) {
-      if (lane == 0) { S.s_vc0[wid] = vc0; S.s_wc0[wid] = wc0; }
+      if (lane == 0) { put(S.s_vc0[wid], vc0); put(S.s_wc0[wid], wc0); }
       gsync(bar_id);
       if (lane == 31) {
         vcn = (wid + 1 < NW) ? S.s_vc0[wid + 1] : 0.0;
@@ -589,14 +611,14 @@ struct Propagator {
     R K1b[L2 > 0 ? L2 : 1], K2b[L2 > 0 ? L2 : 1];
     R iB2;
     if (NW > 1) {
-      if (lane == 0) { S.s_vw0[wid] = vw; S.s_ww0[wid] = ww; }
+      if (lane == 0) { put(S.s_vw0[wid], vw); put(S.s_ww0[wid], ww); }
       gsync(bar_id);
       if (lane == 31) {
         vwn = (wid + 1 < NW) ? S.s_vw0[wid + 1] : 0.0;
         wwn = (wid + 1 < NW) ? S.s_ww0[wid + 1] : 0.0;
-        S.s_A[wid] = (wid == 0) ? 0.0 : -al * vw30;
-        S.s_B[wid] = be - al * ww30 - ga * vwn;
-        S.s_C[wid] = (wid + 1 < NW) ? -ga * wwn : 0.0;
+        put(S.s_A[wid], (wid == 0) ? 0.0 : -al * vw30);
+        put(S.s_B[wid], be - al * ww30 - ga * vwn);
+        put(S.s_C[wid], (wid + 1 < NW) ? -ga * wwn : 0.0);
       }
       gsync(bar_id);
       double a = (lane < NW) ? S.s_A[lane] : 0.0;
@@ -649,7 +671,7 @@ struct Propagator {
         const R zw = t * ibw;
         const R zw30 = __shfl_sync(FULL, zw, 30);
         R zwn = (R)0;
-        if (lane == 0) { S.pub_zc0[wid] = zc0; S.pub_zw[wid] = zw; }
+        if (lane == 0) { put(S.pub_zc0[wid], zc0); put(S.pub_zw[wid], zw); }
         gsync(bar_id);
         if (lane == 31) {
           const bool has_next = (wid + 1 < NW);
@@ -659,7 +681,7 @@ struct Propagator {
             zc0n = zcx;
             rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zcl, rl));
           }
-          S.pub_R[wid] = fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho));
+          put(S.pub_R[wid], fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho)));
         }
         gsync(bar_id);
         R t2 = (lane < NW) ? S.pub_R[lane] : (R)0;
@@ -827,7 +849,7 @@ struct Propagator {
       bad |= __shfl_down_sync(FULL, bad, s);
     }
     if (NW > 1) {
-      if (lane == 0) { S.red[wid] = qpart; S.ired[wid] = bad; }
+      if (lane == 0) { put(S.red[wid], qpart); put(S.ired[wid], bad); }
       gsync(bar_id);
       if (P == 0) {
         qpart = 0.0;
@@ -852,6 +874,19 @@ propagate_kernel(BatchDev b, ClassDev cls) {
   const int worker = blockIdx.x * Pp::GPC + g;
   if (worker >= cls.workers) return;
   Pp::run(b, cls, sm[g], P, worker, 1 + g);
+}
+
+// Propagator of one large shape class on thread-block clusters of CL CTAs (one
+// group per cluster; launched with the cluster dimension as a launch attribute).
+template <typename R, int C, int NW, bool DELTA, int CL>
+__global__ void __launch_bounds__(32 * NW / CL, 1) propagate_cluster_kernel(BatchDev b, ClassDev cls) {
+  using Pp = Propagator<R, C, NW, DELTA, CL>;
+  __shared__ GroupSmem<R, NW> sm;
+  const int rank = (int)cooperative_groups::this_cluster().block_rank();
+  const int P = rank * Pp::CTA + (int)threadIdx.x;
+  const int worker = (int)(blockIdx.x / CL);
+  if (worker >= cls.workers) return;  // the same for every CTA of the cluster
+  Pp::run(b, cls, sm, P, worker, 1);
 }
 
 // Fused persistent solve of one shape class (see Propagator::solve).

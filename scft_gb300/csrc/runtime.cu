@@ -305,8 +305,11 @@ static int plan(scft_batch *B, int p, double frac, int paths = 0) {
     c.gpc = propagate_groups_per_cta(c.C, c.NW);
     int budget = (int)std::floor(cost / total * frac * cps * sms + 0.5);
     budget = std::max(1, budget);
-    c.workers = (int)std::min((long long)c.items.size() * (1 + paths), (long long)budget * c.gpc);
-    c.grid = (c.workers + c.gpc - 1) / c.gpc;
+    // cluster classes: one group per cluster of CL CTAs
+    const int CL = cluster_ctas(p == PREC_F64, c.C, c.NW);
+    c.workers = (int)std::min((long long)c.items.size() * (1 + paths),
+                              std::max(1LL, (long long)budget * c.gpc / CL));
+    c.grid = (c.workers + c.gpc - 1) / c.gpc * CL;
     c.slot_elems = (long long)(maxhalf + 1) * 32 * c.NW * c.C;
     const size_t esz = (p == PREC_F32) ? 4 : 8;
     for (;;) {
@@ -316,7 +319,7 @@ static int plan(scft_batch *B, int p, double frac, int paths = 0) {
       c.scratch = nullptr;
       if (c.workers <= 1) return set_err(SCFT_ENOMEM, "propagator scratch: %s", cudaGetErrorString(e));
       c.workers = (c.workers + 1) / 2;
-      c.grid = (c.workers + c.gpc - 1) / c.gpc;
+      c.grid = (c.workers + c.gpc - 1) / c.gpc * CL;
     }
     int rc = dalloc(&c.d_items, c.items.size());
     if (rc) return rc;
@@ -878,6 +881,7 @@ static int solve_fused_enqueue(scft_batch *B, const scft_solve_opts *o) {
     if (occ <= 0) return set_err(SCFT_ECUDA, "fused solve of class (%d, %d) does not fit an SM", c.C, c.NW);
     if (pocc > occ) grid = std::max(1, (int)((long long)c.grid * occ / pocc));
     d.workers = std::min(c.workers, grid * c.gpc);
+    grid = std::min(grid, (d.workers + c.gpc - 1) / c.gpc);
     CK(cudaEventRecord(B->ev_live[2 * li], s));
     CK(solve_dispatch(c.C, c.NW, b, d, m, grid, s, nullptr));
     g_launches++;
@@ -1031,9 +1035,16 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   if (B->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
   const bool verify = (p == PREC_F32) && o->verify64;
   const bool need64 = (p == PREC_F64) || verify || o->finish_stall > 0;
-  const bool fused = o->fused && p == PREC_F32 && !verify;
+  bool fused = o->fused && p == PREC_F32 && !verify;
   int rc = plan(B, p, 1.0, (fused && o->finish_stall == 0) ? o->forks : 0);
   if (rc) return rc;
+  // Classes that run as thread-block clusters (the default shapes above 2048
+  // interior unknowns) have no fused form: their one-CTA group would spill
+  // registers.
+  // Such batches take the batch-wide form.
+  for (const auto &c : B->plans[p])
+    if (cluster_ctas(p == PREC_F64, c.C, c.NW) > 1) fused = false;
+  if (!fused && B->plan_paths[p] != 0 && (rc = plan(B, p, 1.0, 0))) return rc;
   if ((rc = ensure_mix(B, o->depth, fused ? o->forks : 0))) return rc;
   if (fused) return solve_fused(B, o, res);
   if (p == PREC_F32 && need64 && (rc = plan(B, PREC_F64, 0.125))) return rc;

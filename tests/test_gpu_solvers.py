@@ -311,3 +311,21 @@ def test_non_finite_field_is_flagged_and_the_rest_converge():
         assert r["status"][5] & 2 and not r["status"][5] & ST_CONVERGED
         others = np.delete(r["status"], 5)
         assert np.all(others & ST_CONVERGED)
+
+
+def test_cluster_class_batch_takes_the_batchwide_form():
+    """An instance above 2048 interior unknowns runs its propagator as a
+    thread-block cluster, which has no fused form: a default (fused) solve of a
+    batch holding one takes the batch-wide form, bit-identical to asking for it."""
+    insts = [W.instance(3000, 6.0, 512, 7, 0), W.instance(100, 4.0, 512, 7, 1)]
+    outs = []
+    with api.Batch(insts) as b:
+        for fused in (1, 0):
+            b.reset()
+            r = b.solve(api.solve_opts(precision=F32, tol=1e-6, fused=fused))
+            outs.append((r, b.get()[0]))
+    (r1, w1), (r0, w0) = outs
+    assert np.all(r1["status"] & ST_CONVERGED)
+    np.testing.assert_array_equal(r1["iterations"], r0["iterations"])
+    for a, c in zip(w1, w0):
+        np.testing.assert_array_equal(a, c)
