@@ -260,7 +260,7 @@ def ours_arm(args):
     insts, desc = make_workload(args.workload, args.count)
     mine = [insts[i] for i in shard(insts, rank, world)]
     # forked paths for the noise-driven tail of the warm-started batch (3 paths
-    # from update 28 at an error <= 1e-5); off for the cold start, whose slow
+    # from update 34 at an error <= 1e-5); off for the cold start, whose slow
     # instances are slow for other reasons
     opts = api.solve_opts(precision=F32, tol=TOL, forks=0 if args.cold else 3)
     b = api.Batch(mine)

@@ -1723,8 +1723,8 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->finish_tol = 1e-4;
   o->budget_ms = 0.0;
   o->forks = 0;
-  o->fork_at = 28;
-  o->fork_grace = 10;
+  o->fork_at = 34;
+  o->fork_grace = 6;
   o->fork_first = 1;
   o->fork_err = 1e-5;
   o->fork_scale[0] = 0.9;
