@@ -1039,9 +1039,8 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   int rc = plan(B, p, 1.0, (fused && o->finish_stall == 0) ? o->forks : 0);
   if (rc) return rc;
   // Classes that run as thread-block clusters (the default shapes above 2048
-  // interior unknowns) have no fused form: their one-CTA group would spill
-  // registers.
-  // Such batches take the batch-wide form.
+  // interior unknowns) have no fused form, whose one-CTA group would spill
+  // registers: such batches take the batch-wide form.
   for (const auto &c : B->plans[p])
     if (cluster_ctas(p == PREC_F64, c.C, c.NW) > 1) fused = false;
   if (!fused && B->plan_paths[p] != 0 && (rc = plan(B, p, 1.0, 0))) return rc;
