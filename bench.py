@@ -586,32 +586,28 @@ def config_legs(ws):
                                 "peak_source": kind}
 
     # the graded workload solved: 16 instances (one wave of 4-CTA clusters; each
-    # instance's chain of passes decides the time), graded-mesh step, FP32 stopping at the tolerance
-    # itself (these meshes leave a discretisation floor near 5e-7 on ||phi - f0||),
-    # cold and learned starts, every field then checked under the FP64 propagator
+    # instance's chain of passes decides the time), graded-mesh step, FP32 stopping
+    # at the tolerance itself (these meshes leave a discretisation floor near 5e-7
+    # on ||phi - f0||), cold start (the warm-start network, trained on uniform
+    # meshes, leaves graded meshes at their start), then every field checked
+    # under the FP64 propagator
     sub = insts[:16]
     o = api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=400)
-    solves = {}
     with api.Batch(sub) as b:
-        for start in ("cold", "learned"):
-            if start == "learned" and ws is None:
-                continue
-            b.reset()
-            if start == "learned":
-                ws.predict(b)
-            r = b.solve(o)
-            ms = b.last_ms()
-            conv = int(((r["status"] & ST_CONVERGED) != 0).sum())
-            b.evaluate(F64)
-            _, phi64, _ = b.get()
-            e64 = [float(np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max()) for i, d in enumerate(sub)]
-            solves[start] = {"ms": ms, "converged": conv, "value": conv / (ms / 1e3), "unit": UNIT,
-                             "iterations_mean": float(r["iterations"].mean()), "iterations_max": int(r["iterations"].max()),
-                             "fp64_verified": int(sum(e <= TOL for e in e64)), "fp64_err_max": max(e64)}
+        r = b.solve(o)
+        ms = b.last_ms()
+        conv = int(((r["status"] & ST_CONVERGED) != 0).sum())
+        b.evaluate(F64)
+        _, phi64, _ = b.get()
+    e64 = [float(np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max()) for i, d in enumerate(sub)]
     out["batch_graded_solve"] = {"workload": "16 instances of the graded workload, FP32 solve to 1e-6 "
                                              "(FP32 stop at 1e-6), graded-mesh step, maxit 400; batch-wide form "
                                              "with the 4-CTA cluster propagator",
-                                 "instances": len(sub), **solves}
+                                 "instances": len(sub), "start": "cold", "ms": ms, "converged": conv,
+                                 "value": conv / (ms / 1e3), "unit": UNIT,
+                                 "iterations_mean": float(r["iterations"].mean()),
+                                 "iterations_max": int(r["iterations"].max()),
+                                 "fp64_verified": int(sum(e <= TOL for e in e64)), "fp64_err_max": max(e64)}
     torch.cuda.synchronize()
     return out
 

@@ -306,8 +306,10 @@ int scft_ws_dataset_from_batch(scft_ws *ws, scft_batch *b, const int *mask);
    decaying from lr to lr/50 on a cosine; losses (steps floats, may be NULL)
    receives the minibatch losses. */
 int scft_ws_train(scft_ws *ws, int steps, int batch, float lr, unsigned long long seed, float *losses);
-/* Overwrite every field of b with the network's prediction (on b's stream;
-   scft_batch_last_ms reports its device time). */
+/* Overwrite the fields of b with the network's prediction (on b's stream;
+   scft_batch_last_ms reports its device time).  Instances whose mesh has
+   largest / smallest element above 16 (outside the network's training set of
+   uniform meshes) keep their field. */
 int scft_ws_predict(scft_ws *ws, scft_batch *b);
 const char *scft_ws_last_error(void);
 

@@ -192,7 +192,12 @@ struct WsBatchView {
   const long long *node_off;
   const double *x, *f0;
   double *w;
+  const double *spacing;  // largest / smallest element of each mesh (null: all predicted)
 };
+
+// The network is trained on uniform meshes: instances whose mesh is graded
+// beyond this spacing ratio keep their field (the plain start).
+constexpr double WS_MAX_SPACING_RATIO = 16.0;
 
 // Network input of instance i on the 256-point grid u_k = k/255:
 //   [2u-1, (L-6)/4, (log2 nsteps - 10.5)/1.5, ln(max(f0(x_k), 1e-8))/10]
@@ -220,6 +225,7 @@ __global__ void features_kernel(WsBatchView v, const int *sel, int B, float *fea
 __global__ void predict_fields_kernel(WsBatchView v, const float *out, int B) {
   const int b = blockIdx.x;
   if (b >= B) return;
+  if (v.spacing && v.spacing[b] > WS_MAX_SPACING_RATIO) return;
   const int n = v.n[b];
   const long long off = v.node_off[b];
   const double *x = v.x + off;
@@ -368,6 +374,7 @@ static WsBatchView ws_view(scft_batch *b) {
   v.x = b->d_x;
   v.f0 = b->d_f0;
   v.w = b->d_w;
+  v.spacing = b->d_spacing;
   return v;
 }
 

@@ -73,3 +73,19 @@ def test_training_reduces_loss_and_warm_start_saves_iterations():
     assert warm["iterations"].mean() < 0.8 * cold["iterations"].mean(), (
         warm["iterations"].mean(), cold["iterations"].mean())
     ws.close()
+
+
+def test_graded_meshes_keep_their_start():
+    """The network is trained on uniform meshes: predicting over a batch leaves
+    the field of an instance graded beyond a spacing ratio of 16 untouched and
+    replaces the others."""
+    import os
+    insts = [W.instance(200, 5.0, 1024, 9, 0), W.instance(512, 5.0, 1024, 9, 1, graded=1.032)]
+    ws = WarmStart(bf16=True)
+    ws.load(os.path.join(os.path.dirname(__file__), "..", "scft_gb300", "weights", "warmstart_w0.npz"))
+    with api.Batch(insts) as b:
+        w_before = b.get()[0]
+        ws.predict(b)
+        w_after = b.get()[0]
+    assert np.abs(w_after[0] - w_before[0]).max() > 1e-3
+    np.testing.assert_array_equal(w_after[1], w_before[1])
