@@ -43,14 +43,17 @@ cudaError_t dispatch_class(const BatchDev &b, const ClassDev &cls, int grid, cud
   using Pp = Propagator<R, C, NW, DELTA>;
   if (exists) { *exists = true; return cudaSuccess; }
   constexpr int CL = cluster_ctas(std::is_same<R, double>::value, C, NW);
-  if constexpr (CL > 1) return dispatch_cluster<R, C, NW, DELTA, CL>(b, cls, grid, st, ctas_per_sm);
-  if (ctas_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, propagate_kernel<R, C, NW, DELTA>,
-                                                         Pp::CTA, 0);
+  if constexpr (CL > 1) {
+    return dispatch_cluster<R, C, NW, DELTA, CL>(b, cls, grid, st, ctas_per_sm);
+  } else {  // the one-CTA kernel is instantiated only for the shapes that use it
+    if (ctas_per_sm) {
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, propagate_kernel<R, C, NW, DELTA>,
+                                                           Pp::CTA, 0);
+    }
+    if (grid <= 0) return cudaSuccess;
+    propagate_kernel<R, C, NW, DELTA><<<grid, Pp::CTA, 0, st>>>(b, cls);
+    return cudaGetLastError();
   }
-  if (grid <= 0) return cudaSuccess;
-  propagate_kernel<R, C, NW, DELTA><<<grid, Pp::CTA, 0, st>>>(b, cls);
-  return cudaGetLastError();
 }
 
 // Fused solve of one shape class: occupancy query or persistent launch.
