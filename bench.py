@@ -599,6 +599,11 @@ def config_legs(ws):
         conv = int(((r["status"] & ST_CONVERGED) != 0).sum())
         b.evaluate(F64)
         _, phi64, _ = b.get()
+        # the plain FP64 form on the same batch: FP64 propagator, same mixing
+        b.reset()
+        r64 = b.solve(api.solve_opts(precision=F64, tol=TOL, maxit=400))
+        ms64 = b.last_ms()
+        conv64 = int(((r64["status"] & ST_CONVERGED) != 0).sum())
     e64 = [float(np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max()) for i, d in enumerate(sub)]
     out["batch_graded_solve"] = {"workload": "16 instances of the graded workload, FP32 solve to 1e-6 "
                                              "(FP32 stop at 1e-6), graded-mesh step, maxit 400; batch-wide form "
@@ -607,7 +612,10 @@ def config_legs(ws):
                                  "value": conv / (ms / 1e3), "unit": UNIT,
                                  "iterations_mean": float(r["iterations"].mean()),
                                  "iterations_max": int(r["iterations"].max()),
-                                 "fp64_verified": int(sum(e <= TOL for e in e64)), "fp64_err_max": max(e64)}
+                                 "fp64_verified": int(sum(e <= TOL for e in e64)), "fp64_err_max": max(e64),
+                                 "plain_fp64": {"ms": ms64, "converged": conv64, "value": conv64 / (ms64 / 1e3),
+                                                "unit": UNIT, "iterations_mean": float(r64["iterations"].mean())},
+                                 "speedup_vs_plain_fp64": (conv / (ms / 1e3)) / max(conv64 / (ms64 / 1e3), 1e-12)}
     torch.cuda.synchronize()
     return out
 
