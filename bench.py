@@ -10,7 +10,15 @@ is converged solves per second of the whole job, device-timed with CUDA events
 on the library's stream; `e2e` repeats the measurement through the public C ABI
 with host buffers (batch creation from the caller's concatenated host arrays
 with its host-to-device copies, solve, and the device-to-host read of fields and
-densities inside the timed region).
+densities inside the timed region).  On the warm-started batch, instances
+still running after update 34 race three forked mixing paths on idle thread
+groups (the outcome depends only on iteration counts).
+
+After the timed region, `configs` reports the other workloads, each at its own
+scale: the CPU-runnable 33-node FP64 solve, the 1024-element FP32-vs-FP64 error
+report, the autotuned cold 4096-instance mixed batch, and the graded
+8192-element workload (one propagator pass in GB/s, and 16 instances solved in
+FP32 and in the plain FP64 form).
 
 Under torchrun (N > 1) every rank solves its cost-balanced share of the batch;
 there is no data-path collective ("weak" scaling with the batch split).
