@@ -32,16 +32,25 @@ VECFUNC = C.CFUNCTYPE(None, C.c_int, _dp, _dp, C.c_void_p)
 REF_VECFUNC = C.CFUNCTYPE(None, C.c_int, _dp, _dp)
 
 
+def reference_dir() -> str | None:
+    """Directory of the reference sources that the recipe (oracle/Makefile,
+    variable REF; SCFT_REFERENCE_DIR overrides it) compiles, or None when that
+    directory does not exist on this host."""
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"],
+                       capture_output=True, text=True)
+    d = r.stdout.strip()
+    return d if r.returncode == 0 and d and os.path.isdir(d) else None
+
+
 def build(with_reference: bool | None = None) -> None:
     """Compile the restatement (always) and the reference routines (when the
     reference sources are present)."""
-    ref = os.environ.get("SCFT_REFERENCE_DIR", "/root/reference")
     targets = ["oracle"]
     if with_reference is None:
-        with_reference = os.path.isdir(ref)
+        with_reference = reference_dir() is not None
     if with_reference:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, f"REF={ref}"] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 
 class Problem(C.Structure):
@@ -119,6 +128,8 @@ class Oracle:
         L.or_f0_gauss_wall.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
         L.or_anderson_solve.argtypes = [C.POINTER(Problem), _dp, C.POINTER(MixOpts),
                                         C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.or_anderson_solve_batch.argtypes = [C.POINTER(Problem), C.c_int, _dp, C.POINTER(MixOpts), C.c_int,
+                                              C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
         self.problem_vecfunc = C.cast(L.or_problem_vecfunc, C.c_void_p)
 
     # -- meshes / targets
@@ -258,30 +269,28 @@ class Oracle:
         return rc, w, it.value, err.value
 
 
-def _solve_instance(args):
-    """Worker of cpu_solve_batch: one instance solved by the oracle."""
-    d, kw = args
-    O = Oracle()
-    p = OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d.get("rule", RULE_ROMBERG))
-    rc, w, it, err = O.anderson_solve(p, d["w0"], **kw)
-    return rc, it, err
-
-
 def cpu_solve_batch(instances, workers=None, **kw):
-    """Solve instances on the host cores with the oracle (a process pool started
-    with spawn).  Returns (list of (rc, iters, err), seconds, workers)."""
-    import multiprocessing as mp
+    """Solve instances on the host cores with the oracle: or_anderson_solve on
+    `workers` threads of the C batch driver (each takes the next unsolved
+    instance).  Returns (list of (rc, iters, err), seconds, workers)."""
     import time
 
     workers = workers or os.cpu_count() or 1
-    args = [({k: d[k] for k in ("x", "f0", "ds", "nsteps", "rule", "w0")}, kw) for d in instances]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(workers) as pool:
-        pool.map(_solve_instance, args[:1])  # start-up outside the timing
-        t0 = time.perf_counter()
-        out = pool.map(_solve_instance, args, chunksize=1)
-        dt = time.perf_counter() - t0
-    return out, dt, workers
+    O = Oracle()
+    probs = [OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d.get("rule", RULE_ROMBERG))
+             for d in instances]
+    arr = (Problem * len(probs))(*[p.c for p in probs])
+    w = np.ascontiguousarray(np.concatenate([np.asarray(d["w0"], dtype=np.float64) for d in instances]))
+    o = dict(MIX_DEFAULTS)
+    o.update(kw)
+    mo = MixOpts(**o)
+    k = len(instances)
+    rc, it, err = (C.c_int * k)(), (C.c_int * k)(), (C.c_double * k)()
+    t0 = time.perf_counter()
+    if O.L.or_anderson_solve_batch(arr, k, _ptr(w), C.byref(mo), int(workers), rc, it, err) != 0:
+        raise RuntimeError("or_anderson_solve_batch: could not start its threads")
+    dt = time.perf_counter() - t0
+    return [(rc[i], it[i], err[i]) for i in range(k)], dt, min(workers, k)
 
 
 class Reference:

@@ -13,6 +13,7 @@
 #include "scft_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1163,4 +1164,52 @@ int or_spline(const double *x, const double *y, int nx, const double *xp, double
   }
   free(lo); free(di); free(up); free(rh); free(M);
   return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* CPU baseline batch driver (threads over independent instances)            */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  const or_problem *p;
+  int count;
+  double *w;
+  const long long *off;
+  const or_mix_opts *o;
+  int *rc, *iters;
+  double *err;
+  int next; /* next unsolved instance, taken with an atomic add */
+} or_batch_job;
+
+static void *or_batch_worker(void *arg) {
+  or_batch_job *J = (or_batch_job *)arg;
+  for (;;) {
+    const int i = __atomic_fetch_add(&J->next, 1, __ATOMIC_RELAXED);
+    if (i >= J->count) break;
+    J->rc[i] = or_anderson_solve(&J->p[i], J->w + J->off[i], J->o, &J->iters[i], &J->err[i]);
+  }
+  return NULL;
+}
+
+int or_anderson_solve_batch(const or_problem *p, int count, double *w, const or_mix_opts *o, int threads,
+                            int *rc, int *iters, double *err) {
+  if (count <= 0) return 0;
+  if (threads < 1) threads = 1;
+  if (threads > count) threads = count;
+  long long *off = (long long *)malloc(sizeof(long long) * (size_t)count);
+  pthread_t *tid = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+  if (!off || !tid) { free(off); free(tid); return -1; }
+  long long acc = 0;
+  for (int i = 0; i < count; i++) { off[i] = acc; acc += p[i].n; }
+  or_batch_job J = {p, count, w, off, o, rc, iters, err, 0};
+  int started = 0, ret = 0;
+  for (int t = 1; t < threads; t++) {
+    if (pthread_create(&tid[t], NULL, or_batch_worker, &J) != 0) { ret = -1; break; }
+    started = t;
+  }
+  or_batch_worker(&J); /* the calling thread works too */
+  for (int t = 1; t <= started; t++) pthread_join(tid[t], NULL);
+  free(off);
+  free(tid);
+  return ret;
 }

@@ -118,6 +118,14 @@ typedef struct or_mix_opts {
 } or_mix_opts;
 int or_anderson_solve(const or_problem *p, double *w, const or_mix_opts *o, int *iters, double *err);
 
+/* The CPU baseline's batch driver: or_anderson_solve of `count` independent
+   instances on `threads` POSIX threads (each thread takes the next unsolved
+   instance from a shared counter).  w: the instances' full nodal fields one
+   after another (node counts p[i].n), solved in place.  rc, iters, err:
+   per-instance outputs.  Returns 0, or -1 when a thread cannot be started. */
+int or_anderson_solve_batch(const or_problem *p, int count, double *w, const or_mix_opts *o, int threads,
+                            int *rc, int *iters, double *err);
+
 /* Cubic spline of the table (x, y) (nx points, x increasing) evaluated at the
    nxp points xp into yp: spline_chen.c:13-106.  m == NULL: not-a-knot end
    conditions (the third derivative is continuous at the second and second-last

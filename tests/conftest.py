@@ -25,9 +25,8 @@ def oracle():
 def reference():
     from oracle import oracle as orc
 
-    if not orc.Reference.available():
-        if os.path.isdir(os.environ.get("SCFT_REFERENCE_DIR", "/root/reference")):
-            orc.build(with_reference=True)
+    if not orc.Reference.available() and orc.reference_dir() is not None:
+        orc.build(with_reference=True)
     if not orc.Reference.available():
         pytest.skip("reference routines not built (reference sources absent on this host)")
     return orc.Reference()

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures of tests/golden/ from the reference.
 
-Run in a checkout that has the reference sources (``SCFT_REFERENCE_DIR``,
-default /root/reference) after ``make -C oracle ref``:
+Run on a host that has the reference sources (where oracle/Makefile looks for
+them: its REF, or ``SCFT_REFERENCE_DIR``) after ``make -C oracle ref``:
 
     python tests/golden/make_golden.py
 
@@ -23,7 +23,9 @@ sys.path.insert(0, ROOT)
 
 from oracle import oracle as orc  # noqa: E402
 
-REF = os.environ.get("SCFT_REFERENCE_DIR", "/root/reference")
+REF = orc.reference_dir()
+if REF is None:
+    raise SystemExit("reference sources not found (set SCFT_REFERENCE_DIR)")
 
 
 def dump(name, obj):

@@ -13,7 +13,9 @@ import pytest
 from scft_gb300 import _lib, api
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
-REF = os.environ.get("SCFT_REFERENCE_DIR", "/root/reference")
+from oracle import oracle as orc
+
+REF = orc.reference_dir()  # reference sources on this host (None when absent)
 
 
 def load(name):
@@ -78,7 +80,7 @@ def test_res_table_in_the_reference_layout(tmp_path):
         api.read_res(str(p), max_rows=8)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree absent")
+@pytest.mark.skipif(REF is None, reason="reference tree absent")
 def test_reference_files_themselves():
     g = load("dealii_N33.json")
     f = api.read_field(os.path.join(REF, "DEALII_SCFT/inputFiles/N=33_for_read.txt"))
