@@ -123,6 +123,20 @@ int scft_broydn(double *x, int n, int *check, scft_vecfunc f);
 void scft_broydn_set_tol(double tol);
 double scft_broydn_get_err(void);
 
+/* The two solvers with the reference's exact signatures, for code that uses
+   their return values unchanged.
+   scft_nr_adm has the signature of adm (adm.c:24-27) and, like it, returns the
+   last map value g(x) (the vector adm calls xnew) in a heap vector laid out as
+   nrutil's vector(flag, n + flag - 1) (nrutil.c:25-33, one element below index
+   flag): free it with the reference's free_vector(v, flag, n + flag - 1) or with
+   scft_nr_free_vector(v, flag).  On an error it returns NULL with *check = 1
+   (scft_last_error tells why).
+   scft_nr_broydn has the signature of broydn (broydn.c:44-46, with NR's float
+   defined as double, nrutil.h:8): void, *check = 1 on failure or error. */
+double *scft_nr_adm(double *x, int n, int *check, scft_vecfunc f, int flag);
+void scft_nr_free_vector(double *v, int flag);
+void scft_nr_broydn(double x[], int n, int *check, scft_vecfunc f);
+
 /* =========================================================================
  * Batched path: thousands of independent instances per launch.
  * ========================================================================= */
@@ -321,23 +335,27 @@ const char *scft_ws_last_error(void);
  * and per-iteration loops that cannot afford cudaMalloc/cudaFree, which can
  * block on or synchronize the whole device.  The caller passes device buffers:
  * x and w (n_nodes doubles: mesh and field, wall values of w ignored), phi
- * (n_nodes doubles, out) and Q (one double, out, may be NULL).  The work is
- * enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the
- * results are ready when that stream has completed; nothing is copied to or
- * from the host.
+ * (n_nodes doubles, out), Q (one double, out, may be NULL) and status (one int,
+ * out, may be NULL: the SCFT_ST_NOT_DOMINANT / SCFT_ST_NONFINITE bits of the
+ * instance, as scft_batch_status reports them; 0 when the density is sound).
+ * Each must be device (or managed) memory; anything else is refused with
+ * SCFT_EINVAL before any launch.  The work is enqueued on `stream` (a
+ * cudaStream_t, NULL for the default stream) and the results are ready when
+ * that stream has completed; nothing is copied to or from the host.
  *
  * The propagator's half-contour store lives in one fixed 32 MiB device array
  * of the library (every GPU that loads the library holds it until the process
  * exits): an instance needs (nsteps/2 + 1) x padded nodes x 4 bytes (FP32) or
  * 8 bytes (FP64); larger instances are rejected with SCFT_EINVAL and a message
- * from scft_last_error().  All calls share that array, so calls whose GPU work
- * overlaps in time (different streams, threads or processes on the same GPU)
- * race and must be serialised by the caller.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture.  Same results as scft_batch_evaluate.
+ * from scft_last_error().  All calls of one process share that array, so calls
+ * whose GPU work overlaps in time (different streams or threads of the process)
+ * race and must be serialised by the caller.  Every call looks up the array's
+ * device address (cudaGetSymbolAddress); the first call on a device may load the
+ * library's device code, so make it before any stream capture.  Same density,
+ * Q and status as scft_batch_evaluate.
  * ========================================================================= */
 int scft_density_noalloc(int n_nodes, const double *x, const double *w, int nsteps, double ds, int rule,
-                         int precision, double *phi, double *Q, void *stream);
+                         int precision, double *phi, double *Q, int *status, void *stream);
 
 /* =========================================================================
  * The reference's field files (host only; no device is needed).
@@ -390,6 +408,10 @@ int scft_spline(int count, const int *nx, const double *x, const double *y, cons
    retries.  This returns the cached blocks of the current device and the cached
    pinned blocks to CUDA and reports the bytes released. */
 long long scft_mem_trim(void);
+/* Allocation counters of the library since load: *requests = device and pinned
+   host blocks requested from the cache above (served from it or new), *cuda_allocs
+   = the cudaMalloc / cudaMallocHost calls among them.  Either may be NULL. */
+void scft_mem_counters(long long *requests, long long *cuda_allocs);
 
 /* Density and Q of every instance of b (FP64) with the given contour scheme and
    field term: SCFT_SCHEME_IRK2 with SCFT_W_CONSISTENT is the propagator of the

@@ -86,6 +86,9 @@ SIGNATURES = {
     "scft_adm_chen": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int,
                                 C.c_int]),
     "scft_broydn": (C.c_int, [_dp, C.c_int, C.POINTER(C.c_int), C.c_void_p]),
+    "scft_nr_adm": (_dp, [_dp, C.c_int, C.POINTER(C.c_int), C.c_void_p, C.c_int]),
+    "scft_nr_free_vector": (None, [_dp, C.c_int]),
+    "scft_nr_broydn": (None, [_dp, C.c_int, C.POINTER(C.c_int), C.c_void_p]),
     "scft_broydn_set_tol": (None, [C.c_double]),
     "scft_broydn_get_err": (C.c_double, []),
     "scft_solve_opts_init": (None, [C.POINTER(ScftSolveOpts)]),
@@ -125,7 +128,8 @@ SIGNATURES = {
     "scft_ws_predict": (C.c_int, [C.c_void_p, C.c_void_p]),
     "scft_ws_last_error": (C.c_char_p, []),
     "scft_density_noalloc": (C.c_int, [C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp,
-                                       C.c_void_p]),
+                                       C.POINTER(C.c_int), C.c_void_p]),
+    "scft_mem_counters": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "scft_field_read": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), _dp, _dp, _dp, _dp]),
     "scft_field_write": (C.c_int, [C.c_char_p, C.c_int, _dp, _dp, C.c_double, C.c_double]),
     "scft_res_read": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), _dp, C.POINTER(C.c_int),

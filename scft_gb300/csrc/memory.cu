@@ -1,4 +1,5 @@
 // memory.cu -- device and pinned-host memory cache of the library (see memory.cuh).
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <unordered_map>
@@ -28,6 +29,8 @@ struct Pool {
   std::multimap<std::pair<int, size_t>, void *> cached;     // (device or -1 for host, size) -> block
   std::unordered_map<void *, std::pair<int, size_t>> live;  // block -> (device, size)
 };
+
+std::atomic<long long> g_requests{0}, g_cuda_allocs{0};
 
 Pool &pool() {
   static Pool *p = new Pool();  // never destroyed: blocks may be released during process exit
@@ -67,6 +70,7 @@ cudaError_t acquire(void **p, size_t bytes, bool host) {
     if (e != cudaSuccess) return e;
   }
   const size_t need = round_size(bytes);
+  g_requests++;
   Pool &P = pool();
   std::lock_guard<std::mutex> g(P.mu);
   size_t got = 0;
@@ -75,10 +79,12 @@ cudaError_t acquire(void **p, size_t bytes, bool host) {
     *p = q;
     return cudaSuccess;
   }
+  g_cuda_allocs++;
   cudaError_t e = host ? cudaMallocHost(p, need) : cudaMalloc(p, need);
   if (e != cudaSuccess) {
     cudaGetLastError();
     release_cached(P, dev);
+    g_cuda_allocs++;
     e = host ? cudaMallocHost(p, need) : cudaMalloc(p, need);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -124,3 +130,8 @@ size_t mem_trim() {
 }  // namespace scft
 
 extern "C" long long scft_mem_trim(void) { return (long long)scft::mem_trim(); }
+
+extern "C" void scft_mem_counters(long long *requests, long long *cuda_allocs) {
+  if (requests) *requests = scft::g_requests.load();
+  if (cuda_allocs) *cuda_allocs = scft::g_cuda_allocs.load();
+}

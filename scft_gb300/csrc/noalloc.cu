@@ -10,7 +10,6 @@
 // inputs and outputs, and the propagator's half-contour store lives in a
 // fixed, file-scope device array instead of memory the library allocates.
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -33,23 +32,15 @@ struct NoAllocMeta {
 };
 static __device__ __align__(256) NoAllocMeta g_meta;
 
-__global__ void noalloc_setup_kernel(NoAllocMeta m) {
+__global__ void noalloc_setup_kernel(NoAllocMeta m, int *status) {
   // Every call reuses g_meta: the work-queue counter and the status must start
   // at zero, the rest is overwritten with this call's instance.
   m.head = 0;
   m.status = 0;
   m.item = 0;
   g_meta = m;
+  if (status) *status = 0;
 }
-
-struct DevicePtrs {
-  bool ready = false;
-  void *scratch = nullptr;
-  NoAllocMeta *meta = nullptr;
-};
-constexpr int kMaxDevices = 64;
-DevicePtrs g_ptrs[kMaxDevices];
-std::mutex g_mu;
 
 }  // namespace
 
@@ -60,12 +51,23 @@ int scft_internal_set_error(int code, const char *msg);
 
 namespace {
 int fail(int code, const std::string &m) { return scft_internal_set_error(code, m.c_str()); }
+
+// Whether p is memory the current device can address as device memory (device
+// or managed allocations); host pointers, freed or unknown addresses are not.
+bool device_pointer(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
 }  // namespace
 
 extern "C" {
 
 int scft_density_noalloc(int n_nodes, const double *x, const double *w, int nsteps, double ds, int rule,
-                         int precision, double *phi, double *Q, void *stream) {
+                         int precision, double *phi, double *Q, int *status, void *stream) {
   if (n_nodes < 3 || nsteps < 1 || !(ds > 0.0) || !x || !w || !phi ||
       (precision != SCFT_F32 && precision != SCFT_F64) ||
       (rule != SCFT_RULE_ROMBERG && rule != SCFT_RULE_TRAPEZOID))
@@ -87,25 +89,28 @@ int scft_density_noalloc(int n_nodes, const double *x, const double *w, int nste
   }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (e != cudaSuccess) {
+    cudaGetLastError();
     return fail(SCFT_ENODEV, "scft_density_noalloc: no usable CUDA device");
-  DevicePtrs p;
-  {
-    // One-time set-up per device: the host-side names of the device arrays
-    // are not device addresses, so ask the runtime for their addresses.
-    std::lock_guard<std::mutex> lk(g_mu);
-    DevicePtrs &d = g_ptrs[dev];
-    if (!d.ready) {
-      e = cudaGetSymbolAddress(&d.scratch, g_scratch);
-      if (e != cudaSuccess) return fail(SCFT_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      void *mp = nullptr;
-      e = cudaGetSymbolAddress(&mp, g_meta);
-      if (e != cudaSuccess) return fail(SCFT_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      d.meta = static_cast<NoAllocMeta *>(mp);
-      d.ready = true;
-    }
-    p = d;
   }
+  // the kernels dereference these: only device (or managed) memory is accepted
+  if (!device_pointer(x) || !device_pointer(w) || !device_pointer(phi) || (Q && !device_pointer(Q)) ||
+      (status && !device_pointer(status)))
+    return fail(SCFT_EINVAL, "scft_density_noalloc: x, w, phi, Q and status must be device memory");
+  // Host code names the device arrays by host-side stand-ins, not device
+  // addresses: ask the runtime for their addresses on the current device.  This
+  // is done on every call (it allocates nothing), so a reset or recreated
+  // context never leaves a stale address behind.  The first call on a device may
+  // load the library's device code, which is why it belongs before any stream
+  // capture.
+  void *scratch = nullptr, *mp = nullptr;
+  e = cudaGetSymbolAddress(&scratch, g_scratch);
+  if (e == cudaSuccess) e = cudaGetSymbolAddress(&mp, g_meta);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SCFT_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  }
+  NoAllocMeta *meta = static_cast<NoAllocMeta *>(mp);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int want = precision == SCFT_F32 ? 1 : 2;
   m.n = n_nodes;
@@ -113,28 +118,28 @@ int scft_density_noalloc(int n_nodes, const double *x, const double *w, int nste
   m.ds = ds;
   m.node_off = 0;
   m.active = want;
-  noalloc_setup_kernel<<<1, 1, 0, st>>>(m);
+  noalloc_setup_kernel<<<1, 1, 0, st>>>(m, status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(SCFT_ECUDA, std::string("setup launch: ") + cudaGetErrorString(e));
 
   scft::BatchDev b;
   b.count = 1;
-  b.n = &p.meta->n;
-  b.nsteps = &p.meta->nsteps;
-  b.ds = &p.meta->ds;
-  b.node_off = &p.meta->node_off;
+  b.n = &meta->n;
+  b.nsteps = &meta->nsteps;
+  b.ds = &meta->ds;
+  b.node_off = &meta->node_off;
   b.x = x;
   b.w = w;
   b.phi = phi;
-  b.Q = Q ? Q : &p.meta->Q;
-  b.qw = p.meta->qw;
-  b.active = &p.meta->active;
-  b.status = &p.meta->status;
+  b.Q = Q ? Q : &meta->Q;
+  b.qw = meta->qw;
+  b.active = &meta->active;
+  b.status = status ? status : &meta->status;
   scft::ClassDev c;
-  c.items = &p.meta->item;
+  c.items = &meta->item;
   c.count = 1;
-  c.head = &p.meta->head;
-  c.scratch = p.scratch;
+  c.head = &meta->head;
+  c.scratch = scratch;
   c.slot_elems = slot_elems;
   c.workers = 1;
   c.want = want;

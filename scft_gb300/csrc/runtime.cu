@@ -1573,7 +1573,9 @@ int scft_density(const double *w_nodes, double *phi, double *Q) {
 
 void scft_adm_set_maxit(int maxit) { g_adm_maxit = maxit > 0 ? maxit : 1; }
 
-int scft_adm(double *x, int n, int *check, scft_vecfunc f, int flag) {
+// adm of adm.c:24-313; xnew_out (n doubles, may be NULL) receives the last map
+// value g(x), the vector adm.c returns.
+static int adm_impl(double *x, int n, int *check, scft_vecfunc f, int flag, double *xnew_out) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   if (!x || n <= 0 || !check || !f || (flag != 0 && flag != 1)) return set_err(SCFT_EINVAL, "scft_adm");
   const bool internal = (f == scft_fem_fixedpoint_vf) && g_drop.set && n == g_drop.n - 2;
@@ -1624,9 +1626,40 @@ int scft_adm(double *x, int n, int *check, scft_vecfunc f, int flag) {
     }
   }
   if (!rc) CK(cudaMemcpy(x + flag, d_x, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (!rc && xnew_out) CK(cudaMemcpy(xnew_out, d_xn, n * sizeof(double), cudaMemcpyDeviceToHost));
   dfree(d_x); dfree(d_xn); dfree(d_xh); dfree(d_dh); dfree(d_err); dfree(d_ctl);
   cudaStreamDestroy(st);
   return rc;
+}
+
+int scft_adm(double *x, int n, int *check, scft_vecfunc f, int flag) {
+  return adm_impl(x, n, check, f, flag, nullptr);
+}
+
+double *scft_nr_adm(double *x, int n, int *check, scft_vecfunc f, int flag) {
+  if (check) *check = 1;
+  if (n <= 0 || (flag != 0 && flag != 1)) {
+    set_err(SCFT_EINVAL, "scft_nr_adm");
+    return nullptr;
+  }
+  // laid out like nrutil's vector(flag, n + flag - 1): one spare element below
+  // index flag, so that the reference's free_vector(v, flag, n + flag - 1) frees it
+  double *base = static_cast<double *>(malloc(sizeof(double) * ((size_t)n + 1)));
+  if (!base) {
+    set_err(SCFT_ENOMEM, "scft_nr_adm: host allocation");
+    return nullptr;
+  }
+  double *v = base - flag + 1;
+  if (adm_impl(x, n, check, f, flag, v + flag) != SCFT_OK) {
+    if (check) *check = 1;
+    free(base);
+    return nullptr;
+  }
+  return v;
+}
+
+void scft_nr_free_vector(double *v, int flag) {
+  if (v) free(v + flag - 1);
 }
 
 int scft_adm_chen(scft_vecfunc f, double *x, double tol, int maxit, int n, double lmd, int nn, int final_) {
@@ -1695,6 +1728,10 @@ int scft_broydn(double *x, int n, int *check, scft_vecfunc f) {
   int rc = broydn_impl(E, xv, g_broydn_tol, check);
   memcpy(x + 1, xv.data(), n * sizeof(double));
   return rc;
+}
+
+void scft_nr_broydn(double x[], int n, int *check, scft_vecfunc f) {
+  if (scft_broydn(x, n, check, f) != SCFT_OK && check) *check = 1;
 }
 
 void scft_solve_opts_init(scft_solve_opts *o) {

@@ -100,3 +100,27 @@ def test_fork_options_are_checked():
         b.reset()
         r = b.solve(opts(forks=2, fork_at=1, finish_stall=1, finish_tol=1.0))  # the FP64 hand-off: no forks
         assert np.all(r["status"] & ST_CONVERGED) and not np.any(r["status"] & ST_FORKED)
+
+
+def test_spent_budget_ends_a_forked_solve_while_groups_wait_for_paths():
+    """Groups with nothing left to claim wait for other groups' forks.  A time
+    budget that runs out in the middle of a forked solve must end those waits
+    too: the solve returns promptly, every instance is either converged or
+    stopped with the watchdog bit, and the next solve of the batch is normal."""
+    import time
+
+    insts = W.batch_mixed(64, seed=96)
+    with api.Batch(insts) as b:
+        r0 = b.solve(opts(forks=0))
+        assert np.all(r0["status"] & ST_CONVERGED)
+        b.reset()
+        t = time.perf_counter()
+        r = b.solve(opts(forks=3, fork_at=2, fork_err=1.0, budget_ms=4.0))
+        dt = time.perf_counter() - t
+        st = r["status"]
+        assert np.all((st & ST_CONVERGED) | (st & 32)), st
+        assert np.any(st & 32), "the budget ran out after every instance had finished"
+        assert dt < 20.0
+        b.reset()
+        r2 = b.solve(opts(forks=3, fork_at=2, fork_err=1.0))
+        assert np.all(r2["status"] & ST_CONVERGED) and not np.any(r2["status"] & 32)
