@@ -3,29 +3,35 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-One step solves every instance of the workload to ||phi - f0||_inf <= 1e-6 with
-the batched FP32 propagator and FP64 Anderson mixing (learned warm start when a
-trained network is available), starting from fields resident in HBM.  `value`
-is converged solves per second of the whole job, device-timed with CUDA events
-on the library's stream; `e2e` repeats the measurement through the public C ABI
-with host buffers (batch creation from the caller's concatenated host arrays
-with its host-to-device copies, solve, and the device-to-host read of fields and
-densities inside the timed region).  On the warm-started batch, instances
-still running after update 34 race three forked mixing paths on idle thread
-groups (the outcome depends only on iteration counts).
+One step solves every instance of one 4096-instance batch to ||phi - f0||_inf
+<= 1e-6 with the batched FP32 propagator and FP64 Anderson mixing, learned warm
+start included, starting from fields resident in HBM.  The steps cycle over
+three held-out batches (seeds 47, 48, 49: never used for training, seed 41, or
+for tuning the mixing and forked-path defaults, seeds 43-46).  `value` is
+converged solves per second of the whole job (total converged / total
+device time, CUDA events on the library's stream); `e2e` repeats the
+measurement through the public C ABI with host buffers (batch creation from the
+caller's concatenated host arrays with its host-to-device copies, solve, and the
+device-to-host read of fields and densities inside the timed region).  On the
+warm-started batches, instances still running after update 34 race three forked
+mixing paths on idle thread groups (the outcome depends only on iteration
+counts); `value_without_forks` is the same measurement with forks off.
 
-After the timed region, `configs` reports the other workloads, each at its own
-scale: the CPU-runnable 33-node FP64 solve, the 1024-element FP32-vs-FP64 error
-report, the autotuned cold 4096-instance mixed batch, and the graded
-8192-element workload (one propagator pass in GB/s, and 16 instances solved in
-FP32 and in the plain FP64 form).
+After the timed region the same batches are solved in FP32 from the cold start
+(what the learned part adds), in FP64 from the cold start (the plain FP64 GPU
+form, batched) and, on a sample, one instance per solve (unbatched).  `configs`
+reports the other workloads at their own scale.
 
-Under torchrun (N > 1) every rank solves its cost-balanced share of the batch;
+stdout carries one compact JSON line; the full record (per-class statistics,
+every config's details) goes to stderr as one JSON line before it, and to
+--detail PATH when given.
+
+Under torchrun (N > 1) every rank solves its cost-balanced share of each batch;
 there is no data-path collective ("weak" scaling with the batch split).
 
 --impl reference times the reference's method on the host cores instead: the
 C restatement of its FEM propagator with the same Anderson mixing, one instance
-per worker process, over a bounded sample of the same workload.
+per thread, over a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -151,12 +157,16 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-def make_workload(name: str, count: int | None):
+HELD_OUT_SEEDS = (47, 48, 49)  # warm-start evaluation batches never used for training or tuning
+
+
+def make_workload(name: str, count: int | None, seed: int | None = None):
     from scft_gb300 import workloads as W
 
     if name == "warmstart_eval":
-        return W.warmstart_eval(count or 4096), (
-            f"{count or 4096} held-out instances: elements log-uniform in [64, 512], L ~ U[2, 10], "
+        sd = HELD_OUT_SEEDS[0] if seed is None else seed
+        return W.warmstart_eval(count or 4096, seed=sd), (
+            f"{count or 4096} held-out instances per batch: elements log-uniform in [64, 512], L ~ U[2, 10], "
             "contour steps in {512, 1024, 2048, 4096}, Gaussian-wall target, Romberg density")
     if name == "batch_mixed":
         return W.batch_mixed(count or 4096), (
@@ -167,6 +177,12 @@ def make_workload(name: str, count: int | None):
             f"{count or 512} instances: 8192 elements graded by 1.002 toward both walls, "
             "8192 contour steps, L ~ U[2, 12]")
     raise SystemExit(f"unknown workload {name}")
+
+
+def workload_seeds(name: str):
+    """The batches the steps cycle over: the three held-out seeds for the
+    warm-start evaluation workload, the workload's own seed otherwise."""
+    return list(HELD_OUT_SEEDS) if name == "warmstart_eval" else [None]
 
 
 def instance_bytes(insts):
@@ -249,11 +265,11 @@ def reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded splitmix64 instances)",
-        "config": {"workload": desc, "tol": TOL, "sample": f"{len(sample)} of {len(insts)} instances, every "
-                   f"{max(1, len(insts) // args.cpu_sample)}th, cold start", "method": "FP64 implicit-Euler "
-                   "FEM propagator (restated 1D_FEM.c / simple_FEM_1D_transient.m) + safeguarded Anderson"},
+        "config": {"workload": desc, "tol": TOL, "sample": f"{len(sample)} of {len(insts)} instances of seed {HELD_OUT_SEEDS[0]}, cold start",
+                   "method": "FP64 implicit-Euler FEM propagator (restated 1D_FEM.c / simple_FEM_1D_transient.m) "
+                             "+ safeguarded Anderson, one instance per host thread"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nw, "kind": "port",
-                         "sample": f"{len(sample)} instances per step"},
+                         "sample": f"{len(sample)} instances per step", "mixing": CPU_MIXING},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -265,15 +281,21 @@ def ours_arm(args):
     from scft_gb300 import F32, F64, ST_CONVERGED, api
     from scft_gb300.shard import shard
 
-    insts, desc = make_workload(args.workload, args.count)
-    mine = [insts[i] for i in shard(insts, rank, world)]
+    seeds = workload_seeds(args.workload)
+    sets, desc = [], None
+    for sd in seeds:
+        insts, desc = make_workload(args.workload, args.count, sd)
+        sets.append([insts[i] for i in shard(insts, rank, world)])
+    n_inst = sum(len(m) for m in sets) // len(sets)
     # forked paths for the noise-driven tail of the warm-started batch (3 paths
     # from update 34 at an error <= 1e-5); off for the cold start, whose slow
     # instances are slow for other reasons
     opts = api.solve_opts(precision=F32, tol=TOL, forks=0 if args.cold else 3)
-    b = api.Batch(mine)
+    nofork = api.solve_opts(precision=F32, tol=TOL, forks=0)
+    batches = [api.Batch(m) for m in sets]
     if args.autotune:
-        b.autotune(F32)
+        for b in batches:
+            b.autotune(F32)
     ws = None
     if not args.cold and os.path.exists(args.weights):
         from scft_gb300.warmstart import WarmStart
@@ -290,8 +312,26 @@ def ours_arm(args):
             batch.reset()
         return batch.last_ms()
 
+    def run_steps(o, steps, live=None, its=None):
+        """`steps` solves cycling over the batches: (total ms, total converged)."""
+        tot_ms, tot_conv = 0.0, 0
+        for k in range(steps):
+            b = batches[k % len(batches)]
+            t_start = start_fields(b)
+            r = b.solve(o)
+            tot_ms += t_start + b.last_ms()
+            tot_conv += int(((r["status"] & ST_CONVERGED) != 0).sum())
+            if live is not None:
+                for c in b.live_stats(F32):
+                    a = live.setdefault((c["C"], c["NW"]), [0, 0.0, 0.0])
+                    a[0] += c["launches"]; a[1] += c["bytes"]; a[2] += c["ms"]
+            if its is not None:
+                its.append(r)
+        return tot_ms, tot_conv
+
     # warm-up
-    for _ in range(args.warmup):
+    for k in range(max(args.warmup, len(batches))):
+        b = batches[k % len(batches)]
         start_fields(b)
         b.solve(opts)
     torch.cuda.synchronize()
@@ -299,100 +339,96 @@ def ours_arm(args):
     clocks = Clocks(local)
     clocks.start()
     l0 = api.kernel_launches()
-    step_ms, conv, iters = [], [], []
-    live = {}
-    for _ in range(args.steps):
-        t_start = start_fields(b)
-        r = b.solve(opts)
-        step_ms.append(t_start + b.last_ms())
-        for c in b.live_stats(F32):
-            a = live.setdefault((c["C"], c["NW"]), [0, 0.0, 0.0])
-            a[0] += c["launches"]; a[1] += c["bytes"]; a[2] += c["ms"]
-        conv.append(int(((r["status"] & ST_CONVERGED) != 0).sum()))
-        iters.append(float(r["iterations"].mean()))
-    its_last = r["iterations"]
-    tr_active, tr_ms = b.trace()
+    live, results = {}, []
+    tot_ms, tot_conv = run_steps(opts, args.steps, live, results)
     torch.cuda.synchronize()
     launches = api.kernel_launches() - l0
     clk = clocks.stop()
     barrier(torch, world)
-    ms_rank = statistics.mean(step_ms)
-    ms = allreduce_max(torch, world, ms_rank)
-    conv_all = allreduce_sum(torch, world, statistics.mean(conv))
+    ms = allreduce_max(torch, world, tot_ms / args.steps)
+    conv_all = allreduce_sum(torch, world, tot_conv / args.steps)
     value = conv_all / (ms / 1e3)
+    its_all = np.concatenate([r["iterations"] for r in results])
 
-    extra = {}
-    # FP64 check of the FP32-converged fields (outside the timed region)
-    w_fp32, _, _ = b.get()
-    b.evaluate(F64)
-    _, phi64, _ = b.get()
-    ok = 0
-    for d, p in zip(mine, phi64):
-        ok += float(abs(p[1:-1] - d["f0"][1:-1]).max()) <= TOL
-    extra["fp64_verified_fraction"] = ok / len(mine)
+    detail = {}
+    # the same batches without forked paths (outside the timed region)
+    nf_steps = max(len(batches), min(args.steps, 2 * len(batches)))
+    nf_ms, nf_conv = run_steps(nofork, nf_steps)
+    value_nofork = allreduce_sum(torch, world, nf_conv / nf_steps) / (
+        allreduce_max(torch, world, nf_ms / nf_steps) / 1e3)
+
+    # FP64 check of the FP32-converged fields of the last step's batch
+    bl = batches[(args.steps - 1) % len(batches)]
+    bl_insts = sets[(args.steps - 1) % len(batches)]
+    bl.evaluate(F64)
+    _, phi64, _ = bl.get()
+    ok = sum(float(abs(p[1:-1] - d["f0"][1:-1]).max()) <= TOL for d, p in zip(bl_insts, phi64))
+    fp64_verified = ok / len(bl_insts)
 
     # roofline of the dominant propagator class: its launches inside the timed
-    # solves (CUDA events recorded around each launch in the solve graphs)
+    # solves (CUDA events recorded around each launch on its stream)
     (dC, dNW), (dl, dby, dms) = max(live.items(), key=lambda kv: kv[1][2])
     peak, peak_kind = peaks()
     achieved = dby / (dms / 1e3) / 1e9
     traffic = committed_traffic(args.workload, dC, dNW, dby / dl, bool(opts.fused))
-    # the same classes, one full pass each with the class alone on the GPU
-    prof = b.profile(F32)
+    kname = (f"solve_kernel<float,{dC},{dNW}>" if opts.fused else f"propagate_kernel<float,{dC},{dNW}>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_kind,
-                "kernel": (f"solve_kernel<float,C={dC},NW={dNW}> (fused contour passes and Anderson steps)"
-                           if opts.fused else f"propagate_kernel<float,C={dC},NW={dNW},increment form>"),
-                "launches": dl, "bytes_per_launch": dby / dl, "ms_per_launch": dms / dl,
-                "live_classes": [{"C": k[0], "NW": k[1], "launches": v[0], "bytes": v[1], "ms": v[2],
-                                  "GBps": v[1] / (v[2] / 1e3) / 1e9 if v[2] > 0 else None}
-                                 for k, v in sorted(live.items())],
-                "alone_classes": prof}
+                "traffic": traffic, "peak_source": peak_kind, "kernel": kname, "launches": dl,
+                "bytes_per_launch": dby / dl, "ms_per_launch": dms / dl}
+    detail["live_classes"] = [{"C": k[0], "NW": k[1], "launches": v[0], "bytes": v[1], "ms": v[2],
+                               "GBps": v[1] / (v[2] / 1e3) / 1e9 if v[2] > 0 else None}
+                              for k, v in sorted(live.items())]
+    detail["alone_classes"] = batches[0].profile(F32)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 propagator, f64 mixing/residual",
         "data": "synthetic (seeded splitmix64 instances)",
-        "config": {"workload": desc, "instances": len(insts), "tol": TOL,
-                   "start": ("learned warm start (conv net, weights " + os.path.relpath(args.weights, ROOT) + ")")
-                   if ws is not None else "cold (w0 ~ U[-0.1, 0.1])",
-                   "l2": "working set (half-contour stores of concurrent instances) larger than L2",
-                   "mixing": "Anderson depth 10, beta 1.0, ln-residual with (1 - 0.6 d2/dx2) preconditioner"
-                             + (f"; instances still running after {opts.fork_at} updates fork (at an error <= "
-                                f"{opts.fork_err:g}) into {opts.forks} paths (beta x "
-                                f"{', '.join(str(opts.fork_scale[k]) for k in range(opts.forks))}); the own path "
-                                f"wins if converged within {opts.fork_grace} updates of the fork, else the path "
-                                "with the fewest iterations" if opts.forks else ""),
+        "config": {"workload": desc, "instances": n_inst * world, "seeds": seeds, "tol": TOL,
+                   "start": "learned warm start" if ws is not None else "cold (w0 ~ U[-0.1, 0.1])",
+                   "forks": (f"{opts.forks} paths after update {opts.fork_at}" if opts.forks else "off"),
+                   "l2": "half-contour stores of concurrent instances exceed L2",
                    "parallelism": f"replicas x{world}, batch split by cost"},
         "gpu_launches": launches,
-        "iterations_mean": statistics.mean(iters),
-        "iterations_pct": {q: float(np.percentile(its_last, q)) for q in (50, 90, 99, 100)},
-        "tail": {"ms_until_90pct_done": float(tr_ms[int(np.argmax(tr_active <= 0.1 * len(mine)))])
-                 if len(tr_ms) and (tr_active <= 0.1 * len(mine)).any() else None,
-                 "ms_total_host": float(tr_ms[-1]) if len(tr_ms) else None},
-        "converged_per_step": conv_all,
-        "status_last_step": {name: int(((r["status"] & bit) != 0).sum()) for name, bit in
-                             (("converged", 4), ("max_iterations", 8), ("non_finite", 2), ("not_dominant", 1),
-                              ("restarted", 16), ("watchdog", 32), ("forked_winner", 128))},
+        "value_without_forks": value_nofork,
+        "fp64_verified_fraction": fp64_verified,
+        "iterations": {"mean": float(its_all.mean()),
+                       **{f"p{q}": float(np.percentile(its_all, q)) for q in (50, 90, 99, 100)}},
         "clocks": clk,
         "roofline": roofline,
     }
-    line.update(extra)
 
     if rank == 0 and world == 1 and not args.no_plain64:
+        # what the learned part adds: the same batches, FP32, cold start
+        cold_ms, cold_conv, cold_its = 0.0, 0, []
+        o32c = api.solve_opts(precision=F32, tol=TOL, forks=0)
+        for b in batches:
+            b.reset()
+            r = b.solve(o32c)
+            cold_ms += b.last_ms()
+            cold_conv += int(((r["status"] & ST_CONVERGED) != 0).sum())
+            cold_its.append(r["iterations"])
+        v_cold = cold_conv / (cold_ms / 1e3)
+        detail["batched_fp32_cold"] = {"value": v_cold, "unit": UNIT, "ms_per_batch": cold_ms / len(batches),
+                                       "converged": cold_conv,
+                                       "iterations_mean": float(np.concatenate(cold_its).mean())}
+        # the plain FP64 form of the same batches, batched, cold start
         o64 = api.solve_opts(precision=F64, tol=TOL)
-        # the same batch, batched but without the other two patterns: FP64 propagator, cold start
-        b.reset()
-        r64 = b.solve(o64)
-        c64 = int(((r64["status"] & ST_CONVERGED) != 0).sum())
-        line["batched_fp64_cold"] = {"value": c64 / (b.last_ms() / 1e3), "unit": UNIT, "ms": b.last_ms(),
-                                     "converged": c64, "iterations_mean": float(r64["iterations"].mean())}
-        line["speedup_vs_batched_fp64_cold"] = (value / line["batched_fp64_cold"]["value"]
-                                                if c64 else None)
-        # the plain form: one instance per solve (no batching), FP64 propagator, cold start;
-        # device time summed over a strided sample of the same batch
-        sample = cpu_sample(mine, args.plain_sample)
+        f64_ms, f64_conv, f64_its = 0.0, 0, []
+        for b in batches:
+            b.reset()
+            r64 = b.solve(o64)
+            f64_ms += b.last_ms()
+            f64_conv += int(((r64["status"] & ST_CONVERGED) != 0).sum())
+            f64_its.append(r64["iterations"])
+        v64 = f64_conv / (f64_ms / 1e3)
+        detail["batched_fp64_cold"] = {"value": v64, "unit": UNIT, "ms_per_batch": f64_ms / len(batches),
+                                       "converged": f64_conv,
+                                       "iterations_mean": float(np.concatenate(f64_its).mean())}
+        # the plain form: one instance per solve (no batching), FP64, cold start;
+        # device time summed over a strided sample of the first batch
+        sample = cpu_sample(sets[0], args.plain_sample)
         singles = [api.Batch([d]) for d in sample]
         for s1 in singles[:2]:
             s1.reset()
@@ -405,21 +441,26 @@ def ours_arm(args):
             p_conv += int((r1["status"][0] & ST_CONVERGED) != 0)
             p_its.append(int(r1["iterations"][0]))
             s1.close()
-        line["plain_fp64"] = {"value": p_conv / (p_ms / 1e3) if p_ms > 0 else 0.0, "unit": UNIT, "ms": p_ms, "converged": p_conv,
-                              "iterations_mean": float(np.mean(p_its)),
-                              "form": "one instance per solve (no batching), FP64 propagator, cold start, "
-                                      "same Anderson mixing",
-                              "sample": f"{len(sample)} of {len(mine)} instances, every "
-                                        f"{max(1, len(mine) // args.plain_sample)}th"}
-        line["speedup_vs_plain_fp64"] = value / line["plain_fp64"]["value"] if p_conv else None
-    b.close()
+        v_plain = p_conv / (p_ms / 1e3) if p_ms > 0 else 0.0
+        detail["plain_fp64_unbatched"] = {"value": v_plain, "unit": UNIT, "ms": p_ms, "converged": p_conv,
+                                          "iterations_mean": float(np.mean(p_its)),
+                                          "sample": f"{len(sample)} instances of seed {seeds[0]}"}
+        line["vs_forms"] = {
+            "learned_fp32_cold": {"value": v_cold, "speedup": value / v_cold if cold_conv else None,
+                                  "iterations_mean": detail["batched_fp32_cold"]["iterations_mean"]},
+            "batched_fp64_cold": {"value": v64, "speedup": value / v64 if f64_conv else None},
+            "unbatched_fp64_cold": {"value": v_plain, "speedup": value / v_plain if p_conv else None,
+                                    "sample": len(sample)}}
+    for b in batches:
+        b.close()
 
     # end to end through the C ABI with host buffers
     if not args.no_e2e:
-        h2d, d2h = instance_bytes(mine)
-        host = api.Batch.pack(mine)  # the caller's host buffers: node arrays concatenated, as the C ABI takes them
+        h2d, d2h = instance_bytes(sets[0])
+        hosts = [api.Batch.pack(m) for m in sets]  # the caller's host buffers, as the C ABI takes them
         e2e_s, e2e_conv, parts = [], [], []
         for k in range(args.steps + 1):
+            host = hosts[k % len(hosts)]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             with api.Batch.from_arrays(host) as b2:
@@ -439,25 +480,66 @@ def ours_arm(args):
         ec = allreduce_sum(torch, world, statistics.mean(e2e_conv))
         line["e2e"] = {"value": ec / es, "unit": UNIT, "h2d_bytes_per_step": h2d * world,
                        "d2h_bytes_per_step": d2h * world,
-                       "host_ms": {k: 1e3 * statistics.mean(p[i] for p in parts)
+                       "host_ms": {k: round(1e3 * statistics.mean(p[i] for p in parts), 2)
                                    for i, k in enumerate(("create_and_upload", "warm_start_and_solve", "download"))}}
 
     if rank == 0 and world == 1 and not args.no_configs:
-        line["configs"] = config_legs(ws)
-        line["pipelined"] = pipelined_leg(ws, args.workload, opts)
+        detail["configs"] = config_legs(ws)
+        detail["pipelined"] = pipelined_leg(ws, args.workload, opts)
+        line["configs"] = config_summary(detail["configs"], detail["pipelined"])
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = cpu_sample(mine, args.cpu_sample)
+        sample = cpu_sample(sets[0], args.cpu_sample)
         conv_c, dt, nw, _ = run_cpu(sample)
         line["cpu_baseline"] = {"value": conv_c / dt, "unit": UNIT, "cores": nw, "kind": "port",
-                                "sample": f"{len(sample)} of {len(mine)} instances (every "
-                                          f"{max(1, len(mine) // args.cpu_sample)}th), cold start, FP64, "
-                                          f"{dt:.1f} s"}
+                                "sample": f"{len(sample)} of {len(sets[0])} instances of seed {seeds[0]}, "
+                                          f"cold start, FP64, {dt:.1f} s",
+                                "mixing": CPU_MIXING}
     if rank == 0:
+        detail["line"] = line
+        txt = json.dumps(detail)
+        print(txt, file=sys.stderr, flush=True)
+        if args.detail:
+            with open(args.detail, "w") as f:
+                f.write(txt + "\n")
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+CPU_MIXING = ("or_anderson_solve: the batched solver's safeguarded Anderson mixing restated in C (depth 10, "
+              "beta 1, ln-residual with the (1 - 0.6 d2/dx2) preconditioner); the reference's adm_chen "
+              "diverges from these cold starts")
+
+
+def config_summary(c, pipe):
+    """The configs' key figures for the compact stdout line."""
+    out = {}
+    if "single_small_fp64" in c:
+        s = c["single_small_fp64"]
+        out["cfg1_33_nodes_fp64"] = {"gpu_ms": round(s["gpu_ms"], 2), "cpu_ms": round(s["cpu_baseline"]["ms"], 2),
+                                     "iterations": s["iterations"], "err": s["err"]}
+    if "single_large_fp32_vs_fp64" in c:
+        s = c["single_large_fp32_vs_fp64"]
+        out["cfg2_1025_nodes_fp32_vs_fp64"] = {k: s[k] for k in ("phi_err_vs_fp64", "Q_rel_err", "free_energy_err")}
+    if "batch_mixed" in c:
+        s = c["batch_mixed"]
+        out["cfg3_mixed_4096_cold"] = {"value": round(s["value"], 1), "converged": s["converged"]}
+    if "batch_graded_pass" in c:
+        s = c["batch_graded_pass"]
+        out["cfg5_graded_pass"] = {"GBps": round(s["alg_GBps_fp32"], 1), "frac": round(s["frac_of_peak"], 4)}
+    if "batch_graded_solve" in c:
+        s = c["batch_graded_solve"]
+        out["cfg5_graded_solve"] = {k: s[k] for k in ("instances", "start", "converged", "value", "fp64_verified")
+                                    if k in s}
+        if "plain_fp64" in s:
+            out["cfg5_graded_solve"]["plain_fp64"] = {k: s["plain_fp64"][k] for k in ("instances", "converged", "value")
+                                                      if k in s["plain_fp64"]}
+            out["cfg5_graded_solve"]["speedup_vs_plain_fp64"] = s.get("speedup_vs_plain_fp64")
+    if pipe:
+        out["pipelined_4_batches"] = {"value": round(pipe["value"], 1), "value_with_forks": round(pipe["value_with_forks"], 1)}
+    return out
 
 
 def pipelined_leg(ws, workload, opts, nb=4):
@@ -472,7 +554,7 @@ def pipelined_leg(ws, workload, opts, nb=4):
 
     if workload != "warmstart_eval":
         return None
-    bs = [api.Batch(W.warmstart_eval(4096, seed=43 + k)) for k in range(nb)]
+    bs = [api.Batch(W.warmstart_eval(4096, seed=47 + k)) for k in range(nb)]
     plain = api.solve_opts(precision=opts.precision, tol=opts.tol, forks=0)
 
     def run(o):
@@ -684,6 +766,7 @@ def main():
     ap.add_argument("--no-plain64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workload configs")
+    ap.add_argument("--detail", default=None, help="also write the full record (one JSON line) to this file")
     ap.add_argument("--profile-pass", action="store_true", help="one FP32 propagator pass (for ncu)")
     ap.add_argument("--profile-solve", action="store_true", help="one fused FP32 solve (for ncu)")
     args = ap.parse_args()
