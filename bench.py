@@ -166,8 +166,8 @@ def make_workload(name: str, count: int | None, seed: int | None = None):
     if name == "warmstart_eval":
         sd = HELD_OUT_SEEDS[0] if seed is None else seed
         return W.warmstart_eval(count or 4096, seed=sd), (
-            f"{count or 4096} held-out instances per batch: elements log-uniform in [64, 512], L ~ U[2, 10], "
-            "contour steps in {512, 1024, 2048, 4096}, Gaussian-wall target, Romberg density")
+            f"{count or 4096} instances per batch, elements log-uniform in [64, 512], L ~ U[2, 10], "
+            "steps in {512..4096}, Gaussian wall, Romberg")
     if name == "batch_mixed":
         return W.batch_mixed(count or 4096), (
             f"{count or 4096} instances: elements log-uniform in [32, 1024], L ~ U[2, 10], "
@@ -388,7 +388,7 @@ def ours_arm(args):
         "config": {"workload": desc, "instances": n_inst * world, "seeds": seeds, "tol": TOL,
                    "start": "learned warm start" if ws is not None else "cold (w0 ~ U[-0.1, 0.1])",
                    "forks": (f"{opts.forks} paths after update {opts.fork_at}" if opts.forks else "off"),
-                   "l2": "half-contour stores of concurrent instances exceed L2",
+                   "l2": "working set > L2",
                    "parallelism": f"replicas x{world}, batch split by cost"},
         "gpu_launches": launches,
         "value_without_forks": value_nofork,
@@ -502,15 +502,24 @@ def ours_arm(args):
         if args.detail:
             with open(args.detail, "w") as f:
                 f.write(txt + "\n")
-        print(json.dumps(line), flush=True)
+        print(json.dumps(compact(line)), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
-CPU_MIXING = ("or_anderson_solve: the batched solver's safeguarded Anderson mixing restated in C (depth 10, "
-              "beta 1, ln-residual with the (1 - 0.6 d2/dx2) preconditioner); the reference's adm_chen "
-              "diverges from these cold starts")
+CPU_MIXING = "or_anderson_solve (the GPU's Anderson mixing in C; adm_chen diverges from these cold starts)"
+
+
+def compact(v, digits=5):
+    """v with every float rounded to `digits` significant digits (the stdout line)."""
+    if isinstance(v, float):
+        return float(f"{v:.{digits}g}") if np.isfinite(v) else v
+    if isinstance(v, dict):
+        return {k: compact(x, digits) for k, x in v.items()}
+    if isinstance(v, (list, tuple)):
+        return [compact(x, digits) for x in v]
+    return v
 
 
 def config_summary(c, pipe):
