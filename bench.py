@@ -758,6 +758,65 @@ def profile_pass(args):
     return 0
 
 
+def profile_case(args):
+    """Small self-contained runs of the kernels outside the contour loop, for the
+    ncu captures (each after one warm-up):
+      fp64_pass   one FP64 propagator pass (the plain form's propagate_kernel<double>)
+      mix         a batch-wide FP32 solve (mix_kernel after every pass)
+      irk2_block  the deal.II propagator (block_propagate_kernel, IRK2, consistent W)
+      spline      4096 not-a-knot spline tables of 1025 points (spline_kernel)
+      ws_train    warm-start training steps (conv forward, conv_wgrad_kernel, adam_kernel)"""
+    import torch
+
+    from scft_gb300 import F32, F64, SCHEME_IRK2, W_CONSISTENT, api
+    from scft_gb300 import workloads as W
+
+    case, count = args.profile_case, args.count
+    if case == "fp64_pass":
+        insts, _ = make_workload(args.workload, count or 1024)
+        with api.Batch(insts) as b:
+            for _ in range(2):
+                b.evaluate(F64)
+            out = {"ms": b.last_ms(), "classes": b.profile(F64)}
+    elif case == "mix":
+        insts, _ = make_workload(args.workload, count or 1024)
+        with api.Batch(insts) as b:
+            for _ in range(2):
+                b.reset()
+                r = b.solve(api.solve_opts(precision=F32, tol=TOL, fused=0))
+            out = {"ms": b.last_ms(), "iterations_mean": float(r["iterations"].mean())}
+    elif case == "irk2_block":
+        insts = W.batch_mixed(count or 512, seed=11, m_lo=256, m_hi=2048)
+        with api.Batch(insts) as b:
+            for _ in range(2):
+                b.evaluate_scheme(SCHEME_IRK2, W_CONSISTENT)
+            out = {"ms": b.last_ms()}
+    elif case == "spline":
+        rng = np.random.default_rng(7)
+        tables = []
+        for k in range(count or 4096):
+            x = np.sort(rng.uniform(0.0, 4.0, 1025))
+            tables.append((x, np.sin(x * (1 + k % 7)), np.linspace(x[0], x[-1], 2049)))
+        for _ in range(2):
+            api.spline(tables)
+        out = {"tables": len(tables)}
+    elif case == "ws_train":
+        from scft_gb300.warmstart import WarmStart
+
+        insts, _ = make_workload(args.workload, count or 4096)
+        ws = WarmStart(bf16=True)
+        with api.Batch(insts) as b:
+            ws.add_dataset(b)
+        ws.train(steps=2, batch=256)
+        losses = ws.train(steps=8, batch=256)
+        out = {"loss": float(losses[-1])}
+    else:
+        raise SystemExit(f"unknown profile case {case}")
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": case, **out}, default=float))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -778,11 +837,15 @@ def main():
     ap.add_argument("--detail", default=None, help="also write the full record (one JSON line) to this file")
     ap.add_argument("--profile-pass", action="store_true", help="one FP32 propagator pass (for ncu)")
     ap.add_argument("--profile-solve", action="store_true", help="one fused FP32 solve (for ncu)")
+    ap.add_argument("--profile-case", default=None,
+                    help="fp64_pass | mix | irk2_block | spline | ws_train: a small run of one kernel (for ncu)")
     args = ap.parse_args()
     if args.profile_pass:
         return profile_pass(args)
     if args.profile_solve:
         return profile_solve(args)
+    if args.profile_case:
+        return profile_case(args)
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     return reference_arm(args) if args.impl == "reference" else ours_arm(args)

@@ -212,6 +212,14 @@ typedef struct scft_solve_opts {
                             to step_cap / ds instead of the whole step scaled (one wall node of a
                             mesh graded to 1e-6 would otherwise throttle every other node) */
   double precond_hfloor;
+  int transfer_stride;/* > 1: instances that share a mesh shape (node count, contour steps, rule and
+                         spacing ratio) are solved in two stages.  Sorted by film width L, every
+                         transfer_stride-th of them (and the widest) is solved first from its own
+                         field; each other one then starts from the field interpolated in L, node by
+                         node, between its two nearest converged first-stage neighbours, and is
+                         solved.  On meshes graded toward the walls, where the field's wall layer
+                         makes any smooth start slower than the cold one, a neighbour's converged
+                         field is a start within a few iterations of the answer.  0 or 1: off */
 } scft_solve_opts;
 
 typedef struct scft_result {
@@ -326,6 +334,14 @@ int scft_ws_train(scft_ws *ws, int steps, int batch, float lr, unsigned long lon
    uniform meshes) keep their field. */
 int scft_ws_predict(scft_ws *ws, scft_batch *b);
 const char *scft_ws_last_error(void);
+/* With BF16 activations the two 64 -> 64 layers run on the tensor cores
+   (tcgen05.mma, BF16 operands from a BF16 copy of the FP32 weights, FP32
+   accumulators in tensor memory); on = 0 selects the CUDA-core convolution
+   (FP32 weights) instead.  Returns the previous setting. */
+int scft_ws_set_tensor_cores(scft_ws *ws, int on);
+/* 0, or the nonzero code a bounded wait of the tensor-core layers recorded
+   since the network was created (that layer's outputs were then not written). */
+int scft_ws_tensor_core_status(scft_ws *ws);
 
 /* =========================================================================
  * Density without any device allocation.  No counterpart in the reference.

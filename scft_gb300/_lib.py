@@ -63,7 +63,8 @@ class ScftSolveOpts(C.Structure):
                 ("finish_stall", C.c_int), ("finish_tol", C.c_double), ("budget_ms", C.c_double),
                 ("forks", C.c_int), ("fork_at", C.c_int), ("fork_grace", C.c_int), ("fork_first", C.c_int),
                 ("fork_err", C.c_double),
-                ("fork_scale", C.c_double * 4), ("graded_ratio", C.c_double), ("precond_hfloor", C.c_double)]
+                ("fork_scale", C.c_double * 4), ("graded_ratio", C.c_double), ("precond_hfloor", C.c_double),
+                ("transfer_stride", C.c_int)]
 
 
 class ScftResult(C.Structure):
@@ -127,6 +128,8 @@ SIGNATURES = {
     "scft_ws_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _fp]),
     "scft_ws_predict": (C.c_int, [C.c_void_p, C.c_void_p]),
     "scft_ws_last_error": (C.c_char_p, []),
+    "scft_ws_set_tensor_cores": (C.c_int, [C.c_void_p, C.c_int]),
+    "scft_ws_tensor_core_status": (C.c_int, [C.c_void_p]),
     "scft_density_noalloc": (C.c_int, [C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp,
                                        C.POINTER(C.c_int), C.c_void_p]),
     "scft_mem_counters": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),

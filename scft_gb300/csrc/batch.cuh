@@ -22,6 +22,10 @@ struct scft_batch {
   std::vector<int> n, nsteps, rule;
   std::vector<double> ds;
   std::vector<double> spacing_ratio;  // largest / smallest element of each mesh
+  std::vector<double> width;          // film width x[n-1] - x[0] of each instance
+  // solves activate only the instances with d_select[i] != 0 while use_select
+  int *d_select = nullptr;
+  bool use_select = false;
   std::vector<long long> node_off, int_off;
   long long total_nodes = 0, total_int = 0;
   // device instance data

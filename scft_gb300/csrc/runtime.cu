@@ -18,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -444,6 +445,29 @@ __global__ void fill_double_kernel(double *a, long long n, double v) {
   if (i < n) a[i] = v;
 }
 // The solve's deadline on the device clock: now + budget.
+// instances outside the selection take no part in the solve
+__global__ void select_kernel(int *active, const int *select, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && !select[i]) active[i] = 0;
+}
+
+// Start of a second-stage instance of a staged solve: its interior field is
+// interpolated in the film width between two solved neighbours of the same
+// mesh shape, node by node: w_i = (1 - t) w_a + t w_b.  One CTA per instance;
+// plan[4k .. 4k+2] = (i, a, b), tt[k] = t.
+__global__ void transfer_kernel(const int *plan, const double *tt, int m, const int *n, const long long *node_off,
+                                double *w) {
+  const int k = blockIdx.x;
+  if (k >= m) return;
+  const int i = plan[4 * k], a = plan[4 * k + 1], bb = plan[4 * k + 2];
+  const double t = tt[k];
+  const int ni = n[i];
+  if (n[a] != ni || n[bb] != ni) return;
+  double *wi = w + node_off[i];
+  const double *wa = w + node_off[a], *wb = w + node_off[bb];
+  for (int j = 1 + threadIdx.x; j < ni - 1; j += blockDim.x) wi[j] = (1.0 - t) * wa[j] + t * wb[j];
+}
+
 __global__ void set_deadline_kernel(unsigned long long *deadline, unsigned long long budget_ns) {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -569,6 +593,7 @@ static void destroy_batch(scft_batch *B) {
   dfree(B->d_Q); dfree(B->d_qw); dfree(B->d_node_off); dfree(B->d_int_off); dfree(B->d_heads);
   dfree(B->d_w0);
   dfree(B->d_spacing);
+  dfree(B->d_select);
   dfree(B->d_win);
   dfree(B->d_fork_it);
   dfree(B->d_fork);
@@ -596,7 +621,7 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
   scft_batch *B = new scft_batch();
   B->count = count;
   B->n.resize(count); B->nsteps.resize(count); B->rule.resize(count); B->ds.resize(count);
-  B->node_off.resize(count); B->int_off.resize(count); B->spacing_ratio.resize(count);
+  B->node_off.resize(count); B->int_off.resize(count); B->spacing_ratio.resize(count); B->width.resize(count);
   for (int p = 0; p < 2; p++) { B->shapeC[p].assign(count, 0); B->shapeNW[p].assign(count, 0); }
   long long no = 0, io = 0;
   for (int i = 0; i < count; i++) {
@@ -626,6 +651,7 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
       }
     }
     B->spacing_ratio[i] = hmax / hmin;
+    B->width[i] = s.x ? s.x[s.n_nodes - 1] - s.x[0] : s.L;
     B->n[i] = s.n_nodes; B->nsteps[i] = s.nsteps; B->rule[i] = s.rule; B->ds[i] = s.ds;
     B->node_off[i] = no; B->int_off[i] = io;
     no += s.n_nodes; io += s.n_nodes - 2;
@@ -757,6 +783,11 @@ static int solve_begin(scft_batch *B, const scft_solve_opts *o, int p, bool veri
   const int c = B->count;
   int rc;
   if ((rc = fill_int(B->d_active, c, p == PREC_F32 ? 1 : 2, st))) return rc;
+  if (B->use_select) {
+    select_kernel<<<(c + 255) / 256, 256, 0, st>>>(B->d_active, B->d_select, c);
+    g_launches++;
+    CK(cudaGetLastError());
+  }
   CK(cudaMemsetAsync(B->d_status, 0, c * sizeof(int), st));
   CK(cudaMemsetAsync(B->d_iters, 0, c * sizeof(int), st));
   CK(cudaMemsetAsync(B->d_hcount, 0, c * sizeof(int), st));
@@ -1015,7 +1046,7 @@ static int check_opts(const scft_solve_opts *o) {
   const int p = o->precision;
   if ((p != PREC_F32 && p != PREC_F64) || o->depth < 1 || o->depth > 16 || o->maxit < 0 || !(o->tol > 0) ||
       !(o->beta > 0.0 && o->beta <= 1.0) || o->finish_stall < 0 || !(o->budget_ms >= 0.0) ||
-      !(o->graded_ratio >= 0.0) || !(o->precond_hfloor >= 0.0))
+      !(o->graded_ratio >= 0.0) || !(o->precond_hfloor >= 0.0) || o->transfer_stride < 0)
     return set_err(SCFT_EINVAL, "solve options");
   if (o->forks < 0 || o->forks > SCFT_MAX_FORKS)
     return set_err(SCFT_EINVAL, "solve options: forks must be in [0, %d]", SCFT_MAX_FORKS);
@@ -1058,6 +1089,107 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   CK(cudaEventSynchronize(B->t1));
   CK(cudaEventElapsedTime(&B->last_ms, B->t0, B->t1));
   return solve_results(B, res);
+}
+
+// Staged solve (transfer_stride > 1).  Instances that share a mesh shape (node
+// count, contour steps, rule and spacing ratio to 1 %) are sorted by film width;
+// every stride-th of them and the widest are solved first, each from its own
+// field.  Every other one then starts from the field interpolated in the width,
+// node by node, between its nearest converged first-stage neighbours below and
+// above (one of them when only one converged; its own field when neither did),
+// and the second stage solves those.  Groups of fewer than three instances are
+// solved in the first stage.
+static int solve_staged(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
+  const int c = B->count, stride = o->transfer_stride;
+  std::map<std::tuple<int, int, int, long>, std::vector<int>> groups;
+  for (int i = 0; i < c; i++)
+    groups[{B->n[i], B->nsteps[i], B->rule[i], std::lround(std::log(B->spacing_ratio[i]) * 100.0)}].push_back(i);
+  std::vector<int> first(c, 1), below(c, -1), above(c, -1);
+  for (auto &kv : groups) {
+    auto &g = kv.second;
+    if (g.size() < 3) continue;
+    std::stable_sort(g.begin(), g.end(), [&](int a, int b) { return B->width[a] < B->width[b]; });
+    const int m = (int)g.size();
+    for (int r = 0; r < m; r++) first[g[r]] = (r % stride == 0 || r == m - 1) ? 1 : 0;
+    int last = -1;
+    for (int r = 0; r < m; r++) {
+      if (first[g[r]]) last = g[r];
+      else below[g[r]] = last;
+    }
+    last = -1;
+    for (int r = m - 1; r >= 0; r--) {
+      if (first[g[r]]) last = g[r];
+      else above[g[r]] = last;
+    }
+  }
+  if (!B->d_select) {
+    int rc = dalloc(&B->d_select, (size_t)c);
+    if (rc) return rc;
+  }
+  std::vector<scft_result> r1(c), r2(c);
+  auto run_stage = [&](const std::vector<int> &sel, std::vector<scft_result> &out, float *ms) -> int {
+    CK(cudaMemcpy(B->d_select, sel.data(), c * sizeof(int), cudaMemcpyHostToDevice));
+    B->use_select = true;
+    scft_solve_opts os = *o;
+    os.transfer_stride = 0;
+    const int rc = solve(B, &os, out.data());
+    B->use_select = false;
+    *ms = B->last_ms;
+    return rc;
+  };
+  float ms1 = 0.f, ms2 = 0.f, msx = 0.f;
+  int rc = run_stage(first, r1, &ms1);
+  if (rc) return rc;
+  // second-stage starts from the converged first-stage neighbours
+  std::vector<int> second(c, 0), tplan;
+  std::vector<double> tt;
+  for (int i = 0; i < c; i++) {
+    if (first[i]) continue;
+    second[i] = 1;
+    int a = below[i], b = above[i];
+    const bool ca = a >= 0 && (r1[a].status & SCFT_ST_CONVERGED), cb = b >= 0 && (r1[b].status & SCFT_ST_CONVERGED);
+    if (!ca && !cb) continue;
+    if (!ca) a = b;
+    if (!cb) b = a;
+    const double span = B->width[b] - B->width[a];
+    double t = span > 0.0 ? (B->width[i] - B->width[a]) / span : 0.0;
+    t = std::min(1.0, std::max(0.0, t));
+    tplan.insert(tplan.end(), {i, a, b, 0});
+    tt.push_back(t);
+  }
+  if (!tt.empty()) {
+    const int m = (int)tt.size();
+    int *d_plan = nullptr;
+    double *d_t = nullptr;
+    if ((rc = dalloc(&d_plan, tplan.size())) || (rc = dalloc(&d_t, tt.size()))) {
+      dfree(d_plan);
+      return rc;
+    }
+    CK(cudaMemcpyAsync(d_plan, tplan.data(), tplan.size() * sizeof(int), cudaMemcpyHostToDevice, B->st));
+    CK(cudaMemcpyAsync(d_t, tt.data(), tt.size() * sizeof(double), cudaMemcpyHostToDevice, B->st));
+    CK(cudaEventRecord(B->t0, B->st));
+    transfer_kernel<<<m, 256, 0, B->st>>>(d_plan, d_t, m, B->d_n, B->d_node_off, B->d_w);
+    g_launches++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(B->t1, B->st));
+    CK(cudaEventSynchronize(B->t1));
+    CK(cudaEventElapsedTime(&msx, B->t0, B->t1));
+    dfree(d_plan);
+    dfree(d_t);
+  }
+  if (std::any_of(second.begin(), second.end(), [](int v) { return v != 0; })) {
+    if ((rc = run_stage(second, r2, &ms2))) return rc;
+  }
+  // merged outcome: each instance from its own stage
+  std::vector<int> st(c);
+  for (int i = 0; i < c; i++) {
+    const scft_result &r = first[i] ? r1[i] : r2[i];
+    st[i] = r.status;
+    if (res) res[i] = r;
+  }
+  CK(cudaMemcpy(B->d_status, st.data(), c * sizeof(int), cudaMemcpyHostToDevice));
+  B->last_ms = ms1 + msx + ms2;
+  return SCFT_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1803,7 +1935,13 @@ int scft_batch_solve(scft_batch *b, const scft_solve_opts *opts, scft_result *re
   if (!b) return set_err(SCFT_EINVAL, "scft_batch_solve");
   scft_solve_opts o;
   scft_solve_opts_init(&o);
-  return solve(b, opts ? opts : &o, res);
+  const scft_solve_opts *op = opts ? opts : &o;
+  if (op->transfer_stride > 1) {
+    if (check_opts(op)) return SCFT_EINVAL;
+    if (b->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
+    return solve_staged(b, op, res);
+  }
+  return solve(b, op, res);
 }
 
 int scft_batch_solve_async(scft_batch *b, const scft_solve_opts *opts) {
@@ -1812,8 +1950,9 @@ int scft_batch_solve_async(scft_batch *b, const scft_solve_opts *opts) {
   scft_solve_opts_init(&d);
   const scft_solve_opts *o = opts ? opts : &d;
   if (check_opts(o)) return SCFT_EINVAL;
-  if (o->precision != PREC_F32 || !o->fused || o->verify64)
-    return set_err(SCFT_EINVAL, "asynchronous solves run the fused FP32 form (fused = 1, verify64 = 0)");
+  if (o->precision != PREC_F32 || !o->fused || o->verify64 || o->transfer_stride > 1)
+    return set_err(SCFT_EINVAL,
+                   "asynchronous solves run the fused FP32 form (fused = 1, verify64 = 0, transfer_stride <= 1)");
   if (b->pending) return set_err(SCFT_EINVAL, "a solve of this batch is in flight: call scft_batch_wait");
   int rc;
   if ((rc = plan(b, PREC_F32, 1.0, o->finish_stall == 0 ? o->forks : 0)) || (rc = ensure_mix(b, o->depth, o->forks)))

@@ -15,10 +15,12 @@
 #include <cstring>
 #include <random>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "batch.cuh"
 #include "common.cuh"
+#include "conv_tc.cuh"
 #include "memory.cuh"
 #include "scft.h"
 
@@ -261,6 +263,12 @@ struct scft_ws {
   int nparam = 0;
   int poff[WS_LAYERS], boff[WS_LAYERS];
   float *d_p = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr, *d_wt = nullptr;
+  // BF16 activations: the two 64 -> 64 layers run on the tensor cores (tcgen05)
+  // from BF16 weight images repacked at every forward pass; d_tc_err receives a
+  // nonzero code when one of that kernel's bounded waits ran out
+  int tc = 1;
+  __nv_bfloat16 *d_img = nullptr;
+  int *d_tc_err = nullptr;
   int adam_t = 0;
   int cap = 0;
   float *d_feat = nullptr, *d_tgt = nullptr, *d_out = nullptr, *d_gout = nullptr;
@@ -321,8 +329,22 @@ static int ws_forward_dev(scft_ws *W, int B) {
   const float *p = W->d_p;
   const float *nul = nullptr;
   WCK((conv<16, float, TA, float>(W->d_feat, 4, p + W->poff[0], p + W->boff[0], 64, 1, 1, nul, a1, B, W->st)));
-  WCK((conv<16, TA, TA, float>(a1, 64, p + W->poff[1], p + W->boff[1], 64, 2, 1, nul, a2, B, W->st)));
-  WCK((conv<16, TA, TA, float>(a2, 64, p + W->poff[2], p + W->boff[2], 64, 4, 1, nul, a3, B, W->st)));
+  if constexpr (std::is_same<TA, __nv_bfloat16>::value) {
+    if (W->tc) {
+      __nv_bfloat16 *img1 = W->d_img, *img2 = W->d_img + CONV_TC_IMAGE_BYTES / 2;
+      WCK(conv_tc_pack(p + W->poff[1], img1, W->st));
+      WCK(conv_tc_pack(p + W->poff[2], img2, W->st));
+      WCK(conv_tc_forward(a1, img1, p + W->boff[1], 2, 1, a2, B, W->d_tc_err, W->st));
+      WCK(conv_tc_forward(a2, img2, p + W->boff[2], 4, 1, a3, B, W->d_tc_err, W->st));
+      scft_count_launches(4);
+    } else {
+      WCK((conv<16, TA, TA, float>(a1, 64, p + W->poff[1], p + W->boff[1], 64, 2, 1, nul, a2, B, W->st)));
+      WCK((conv<16, TA, TA, float>(a2, 64, p + W->poff[2], p + W->boff[2], 64, 4, 1, nul, a3, B, W->st)));
+    }
+  } else {
+    WCK((conv<16, TA, TA, float>(a1, 64, p + W->poff[1], p + W->boff[1], 64, 2, 1, nul, a2, B, W->st)));
+    WCK((conv<16, TA, TA, float>(a2, 64, p + W->poff[2], p + W->boff[2], 64, 4, 1, nul, a3, B, W->st)));
+  }
   WCK((conv<1, TA, float, float>(a3, 64, p + W->poff[3], p + W->boff[3], 1, 8, 0, nul, W->d_out, B, W->st)));
   return SCFT_OK;
 }
@@ -418,6 +440,9 @@ int scft_ws_create(int act_bf16, unsigned long long seed, scft_ws **out) {
   if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_m, sizeof(float) * off);
   if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_v, sizeof(float) * off);
   if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_wt, sizeof(float) * 64 * 64 * WS_K);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_img, 2 * (size_t)CONV_TC_IMAGE_BYTES);
+  if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_tc_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(W->d_tc_err, 0, sizeof(int), W->st);
   if (e == cudaSuccess) e = scft::mem_alloc((void **)&W->d_loss, sizeof(double) * 65536);
   if (e == cudaSuccess) e = cudaMemcpy(W->d_p, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(W->d_m, 0, sizeof(float) * off);
@@ -434,6 +459,7 @@ int scft_ws_destroy(scft_ws *W) {
   if (!W) return SCFT_OK;
   if (W->st) cudaStreamSynchronize(W->st);
   scft::mem_free(W->d_p); scft::mem_free(W->d_g); scft::mem_free(W->d_m); scft::mem_free(W->d_v); scft::mem_free(W->d_wt);
+  scft::mem_free(W->d_img); scft::mem_free(W->d_tc_err);
   scft::mem_free(W->d_loss); scft::mem_free(W->d_feat); scft::mem_free(W->d_tgt); scft::mem_free(W->d_out); scft::mem_free(W->d_gout);
   for (auto &a : W->d_act) scft::mem_free(a);
   scft::mem_free(W->d_ga); scft::mem_free(W->d_gb); scft::mem_free(W->d_idx); scft::mem_free(W->d_dsf); scft::mem_free(W->d_dst);
@@ -443,6 +469,21 @@ int scft_ws_destroy(scft_ws *W) {
 }
 
 int scft_ws_param_count(scft_ws *W) { return W ? W->nparam : SCFT_EINVAL; }
+
+int scft_ws_set_tensor_cores(scft_ws *W, int on) {
+  if (!W) return ws_err(SCFT_EINVAL, "scft_ws_set_tensor_cores");
+  const int old = W->tc;
+  W->tc = on ? 1 : 0;
+  return old;
+}
+
+int scft_ws_tensor_core_status(scft_ws *W) {
+  if (!W) return ws_err(SCFT_EINVAL, "scft_ws_tensor_core_status");
+  int v = 0;
+  WCK(cudaMemcpyAsync(&v, W->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, W->st));
+  WCK(cudaStreamSynchronize(W->st));
+  return v;
+}
 
 int scft_ws_get_params(scft_ws *W, float *out) {
   if (!W || !out) return ws_err(SCFT_EINVAL, "scft_ws_get_params");

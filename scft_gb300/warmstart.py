@@ -82,6 +82,15 @@ class WarmStart:
                                      _fp(losses)), "scft_ws_train")
         return losses
 
+    def set_tensor_cores(self, on: bool) -> bool:
+        """BF16 networks: the 64 -> 64 layers on the tensor cores (default) or on
+        the CUDA cores; returns the previous setting."""
+        return bool(check(self.lib.scft_ws_set_tensor_cores(self.h, int(bool(on))), "scft_ws_set_tensor_cores"))
+
+    def tensor_core_status(self) -> int:
+        """0, or the code of a bounded wait of the tensor-core layers that ran out."""
+        return check(self.lib.scft_ws_tensor_core_status(self.h), "scft_ws_tensor_core_status")
+
     def predict(self, batch: api.Batch):
         check(self.lib.scft_ws_predict(self.h, batch.h), "scft_ws_predict")
 

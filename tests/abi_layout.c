@@ -24,7 +24,7 @@ int main(void) {
   F(scft_solve_opts, field_floor); F(scft_solve_opts, fused);
   F(scft_solve_opts, finish_stall); F(scft_solve_opts, finish_tol); F(scft_solve_opts, budget_ms);
   F(scft_solve_opts, forks); F(scft_solve_opts, fork_at); F(scft_solve_opts, fork_grace);
-  F(scft_solve_opts, fork_first); F(scft_solve_opts, fork_err);
+  F(scft_solve_opts, fork_first); F(scft_solve_opts, fork_err); F(scft_solve_opts, transfer_stride);
   F(scft_solve_opts, fork_scale); F(scft_solve_opts, graded_ratio); F(scft_solve_opts, precond_hfloor);
   printf("scft_result %zu\n", sizeof(scft_result));
   F(scft_result, status); F(scft_result, iterations); F(scft_result, err); F(scft_result, Q);

@@ -89,3 +89,26 @@ def test_graded_meshes_keep_their_start():
         w_after = b.get()[0]
     assert np.abs(w_after[0] - w_before[0]).max() > 1e-3
     np.testing.assert_array_equal(w_after[1], w_before[1])
+
+
+def test_tensor_core_layers_match_the_cuda_core_layers_and_the_oracle():
+    """With BF16 activations the two 64 -> 64 layers run as tcgen05 GEMMs (BF16
+    operands, FP32 accumulation in tensor memory).  Their network output matches
+    the CUDA-core layers and the FP64 oracle within the BF16 rounding of weights
+    and activations, on two calls in a row, and no bounded wait ran out."""
+    ws = WarmStart(bf16=True, seed=3)
+    p = ws.params()
+    f, _ = rand_inputs(64, seed=2)
+    ref, _ = WO.forward(p, f)
+    scale = max(1.0, float(np.max(np.abs(ref))))
+    assert ws.set_tensor_cores(False)
+    out_cc = ws.forward(f)
+    assert not ws.set_tensor_cores(True)
+    for _ in range(2):
+        out_tc = ws.forward(f)
+        e_ref = float(np.max(np.abs(out_tc - ref))) / scale
+        e_cc = float(np.max(np.abs(out_tc - out_cc))) / scale
+        e_cc_ref = float(np.max(np.abs(out_cc - ref))) / scale
+        assert e_ref <= 2e-2 and e_cc <= 2e-2, (e_ref, e_cc, e_cc_ref)
+    assert ws.tensor_core_status() == 0
+    ws.close()

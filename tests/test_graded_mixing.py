@@ -68,3 +68,83 @@ def test_gpu_graded_batch_converges():
     assert np.all(r["status"] & ST_CONVERGED), r
     for i, d in enumerate(insts):
         assert np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max() <= 2e-6, i
+
+
+def _staged_plan(insts, stride):
+    """CPU restatement of the staged solve's plan (one mesh shape): sorted by
+    film width, every stride-th and the widest solved first; the others start
+    between their nearest first-stage neighbours.  Returns (first, {i: (a, b, t)})."""
+    order = sorted(range(len(insts)), key=lambda i: insts[i]["L"])
+    m = len(order)
+    first = {order[r] for r in range(m) if r % stride == 0 or r == m - 1}
+    plan = {}
+    for r, i in enumerate(order):
+        if i in first:
+            continue
+        a = max((order[q] for q in range(r) if order[q] in first), key=lambda j: insts[j]["L"], default=None)
+        b = min((order[q] for q in range(r + 1, m) if order[q] in first), key=lambda j: insts[j]["L"], default=None)
+        a = b if a is None else a
+        b = a if b is None else b
+        t = 0.0 if insts[b]["L"] == insts[a]["L"] else (insts[i]["L"] - insts[a]["L"]) / (insts[b]["L"] - insts[a]["L"])
+        plan[i] = (a, b, t)
+    return first, plan
+
+
+@pytest.mark.gpu
+def test_gpu_staged_transfer_starts_from_interpolated_neighbours():
+    """transfer_stride: the second-stage instances of a staged solve start from
+    the field interpolated in L between their converged first-stage neighbours.
+    Each one's result is bit-identical to a plain solve started from that field
+    computed on the host, every instance converges and passes the FP64 check, and
+    the transferred starts need fewer iterations than the first stage."""
+    insts = [graded(i, L=3.0 + 0.1 * i) for i in range(21)]
+    stride = 4
+    with api.Batch(insts) as b:
+        r = b.solve(api.solve_opts(precision=F32, tol=2e-6, transfer_stride=stride))
+        w, _, _ = b.get()
+        b.evaluate(F64)
+        _, phi64, _ = b.get()
+    assert np.all(r["status"] & ST_CONVERGED), r["status"]
+    for i, d in enumerate(insts):
+        assert np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max() <= 2e-6, i
+    first, plan = _staged_plan(insts, stride)
+    assert len(first) == 6 and len(plan) == 15
+    second = sorted(plan)
+    starts = []
+    for i in second:
+        a, b_, t = plan[i]
+        s = insts[i]["w0"].copy()
+        s[1:-1] = (1.0 - t) * w[a][1:-1] + t * w[b_][1:-1]
+        starts.append(s)
+    with api.Batch([insts[i] for i in second]) as b2:
+        b2.set_fields(starts)
+        r2 = b2.solve(api.solve_opts(precision=F32, tol=2e-6))
+        w2, _, _ = b2.get()
+    for k, i in enumerate(second):
+        assert r2["iterations"][k] == r["iterations"][i], i
+        np.testing.assert_array_equal(w2[k], w[i])
+    it1 = np.mean([r["iterations"][i] for i in first])
+    it2 = np.mean([r["iterations"][i] for i in second])
+    assert it2 < 0.6 * it1, (it1, it2)
+
+
+@pytest.mark.gpu
+def test_gpu_graded_fp64_hand_off_matches_the_oracle(oracle):
+    """Graded 1024-element meshes (the spacing range of the 8192-element workload
+    at 1/8 of its nodes): FP32 solves with the FP64 hand-off (finish_stall)
+    converge every instance the oracle's FP64 restatement converges, and each
+    field passes the tolerance under the FP64 propagator."""
+    insts = [W.instance(1024, L, 2048, 5, k, graded=1.0161) for k, L in enumerate((3.0, 4.5, 6.0, 8.0))]
+    tol = 2e-6
+    out, _, _ = orc.cpu_solve_batch(insts, workers=len(insts), tol=tol, maxit=600)
+    ok = [rc == 0 for rc, _, _ in out]
+    assert any(ok)
+    with api.Batch(insts) as b:
+        r = b.solve(api.solve_opts(precision=F32, tol=tol, maxit=600, finish_stall=10, finish_tol=1e-4))
+        b.evaluate(F64)
+        _, phi64, _ = b.get()
+    for i, d in enumerate(insts):
+        if ok[i]:
+            assert r["status"][i] & ST_CONVERGED, (i, r["status"][i], r["iterations"][i])
+        if r["status"][i] & ST_CONVERGED:
+            assert np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max() <= tol, i
