@@ -465,7 +465,10 @@ __global__ void transfer_kernel(const int *plan, const double *tt, int m, const 
   if (n[a] != ni || n[bb] != ni) return;
   double *wi = w + node_off[i];
   const double *wa = w + node_off[a], *wb = w + node_off[bb];
-  for (int j = 1 + threadIdx.x; j < ni - 1; j += blockDim.x) wi[j] = (1.0 - t) * wa[j] + t * wb[j];
+  // each product and the sum rounded on its own (no fused multiply-add), as
+  // the same formula evaluates on the host
+  const double s = __dadd_rn(1.0, -t);
+  for (int j = 1 + threadIdx.x; j < ni - 1; j += blockDim.x) wi[j] = __dadd_rn(__dmul_rn(s, wa[j]), __dmul_rn(t, wb[j]));
 }
 
 __global__ void set_deadline_kernel(unsigned long long *deadline, unsigned long long budget_ns) {
