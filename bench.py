@@ -693,7 +693,7 @@ def config_legs(ws):
     # FP32 form from the cold start run on the first 38 instances, one wave of
     # 4-CTA clusters on 152 SMs.
     full = W.batch_graded(512)
-    o = api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=400, transfer_stride=8)
+    o = api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=800, transfer_stride=8)
     with api.Batch(full) as b:
         r = b.solve(o)
         ms = b.last_ms()
@@ -704,8 +704,8 @@ def config_legs(ws):
     wave = 38
     forms = {}
     with api.Batch(full[:wave]) as b:
-        for name, ow in (("plain_fp64_cold", api.solve_opts(precision=F64, tol=TOL, maxit=400)),
-                         ("fp32_cold", api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=400))):
+        for name, ow in (("plain_fp64_cold", api.solve_opts(precision=F64, tol=TOL, maxit=800)),
+                         ("fp32_cold", api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=800))):
             b.reset()
             rw = b.solve(ow)
             cw = int(((rw["status"] & ST_CONVERGED) != 0).sum())
@@ -714,7 +714,7 @@ def config_legs(ws):
     conv = int(ok.sum())
     value = conv / (ms / 1e3)
     out["batch_graded_solve"] = {"workload": "512 instances: 8192 elements graded by 1.002 toward both walls, "
-                                             "8192 steps, L ~ U[2, 12]; FP32 stop at 1e-6, maxit 400, batch-wide "
+                                             "8192 steps, L ~ U[2, 12]; FP32 stop at 1e-6, maxit 800, batch-wide "
                                              "form with the 4-CTA cluster propagator",
                                  "instances": len(full), "start": "transferred (stride 8)", "ms": ms,
                                  "converged": conv, "value": value, "unit": UNIT,
