@@ -12,7 +12,7 @@ import numpy as np
 
 GRID = 256
 K = 5
-LAYERS = [(4, 64, 1, True), (64, 64, 2, True), (64, 64, 4, True), (64, 1, 8, False)]
+LAYERS = [(5, 64, 1, True), (64, 64, 2, True), (64, 64, 4, True), (64, 1, 8, False)]
 SCALE = 5.0
 
 
@@ -35,7 +35,7 @@ def _shifted(x, d):
 
 
 def forward(params, features):
-    """features (B, 4, 256) -> output (B, 256) and the activations."""
+    """features (B, 5, 256) -> output (B, 256) and the activations."""
     acts = [np.asarray(features, dtype=np.float64)]
     for W, b, d, act in unpack(params):
         xs = _shifted(acts[-1], d)
@@ -72,13 +72,15 @@ def loss_grad(params, features, targets):
 
 
 def features(x, f0, nsteps, w=None):
-    """Network input of one instance (4, 256) and the target w/5 on the grid."""
+    """Network input of one instance (5, 256) and the target w/5 on the grid: the
+    grid coordinate, L, log2 of the contour steps, log f0 on the grid and the log
+    of the mean element length."""
     x = np.asarray(x, dtype=np.float64)
     L = x[-1] - x[0]
     u = np.arange(GRID) / (GRID - 1)
     xq = x[0] + u * L
     fq = np.interp(xq, x, f0)
     f = np.stack([2 * u - 1, np.full(GRID, (L - 6.0) / 4.0), np.full(GRID, (np.log2(nsteps) - 10.5) / 1.5),
-                  np.log(np.maximum(fq, 1e-8)) / 10.0])
+                  np.log(np.maximum(fq, 1e-8)) / 10.0, np.full(GRID, np.log(L / (len(x) - 1)) + 3.7)])
     t = None if w is None else np.interp(xq, x, w) / SCALE
     return f, t

@@ -5,7 +5,7 @@
 // reads its initial guesses from files (1D_FEM.c:321-342, scft_util.cc:14-41).
 //
 // Network: NL dilated convolutions over P = 256 grid points, kernel K = 5,
-// dilation 1, 2, 4, 8; channels 4 -> 64 -> 64 -> 64 -> 1; tanh on hidden
+// dilation 1, 2, 4, 8; channels 5 -> 64 -> 64 -> 64 -> 1; tanh on hidden
 // layers; zero padding.  Weights FP32, hidden activations stored BF16 (or FP32
 // for the gradient check), all accumulations FP32.
 #include <cuda_bf16.h>
@@ -27,7 +27,7 @@
 namespace scft {
 
 constexpr int WS_P = 256;        // grid points
-constexpr int WS_IN = 4;         // input features
+constexpr int WS_IN = 5;         // input features
 constexpr int WS_K = 5;          // kernel size
 constexpr int WS_LAYERS = 4;
 constexpr float WS_SCALE = 5.0f; // output scale: w = WS_SCALE * net
@@ -220,6 +220,8 @@ __global__ void features_kernel(WsBatchView v, const int *sel, int B, float *fea
   fb[1 * WS_P + k] = (float)((L - 6.0) / 4.0);
   fb[2 * WS_P + k] = (float)((log2((double)v.nsteps[i]) - 10.5) / 1.5);
   fb[3 * WS_P + k] = (float)(log(fmax(f0, 1e-8)) / 10.0);
+  // mean element length of the mesh: the converged field's wall layer depends on it
+  fb[4 * WS_P + k] = (float)(log(L / (double)(n - 1)) + 3.7);
   if (tgt) tgt[(long long)b * WS_P + k] = (float)(interp_mesh(x, v.w + off, n, xq) / WS_SCALE);
 }
 
@@ -328,7 +330,7 @@ static int ws_forward_dev(scft_ws *W, int B) {
   TA *a1 = (TA *)W->d_act[0], *a2 = (TA *)W->d_act[1], *a3 = (TA *)W->d_act[2];
   const float *p = W->d_p;
   const float *nul = nullptr;
-  WCK((conv<16, float, TA, float>(W->d_feat, 4, p + W->poff[0], p + W->boff[0], 64, 1, 1, nul, a1, B, W->st)));
+  WCK((conv<16, float, TA, float>(W->d_feat, WS_IN, p + W->poff[0], p + W->boff[0], 64, 1, 1, nul, a1, B, W->st)));
   if constexpr (std::is_same<TA, __nv_bfloat16>::value) {
     if (W->tc) {
       __nv_bfloat16 *img1 = W->d_img, *img2 = W->d_img + CONV_TC_IMAGE_BYTES / 2;
@@ -374,8 +376,9 @@ static int ws_backward_dev(scft_ws *W, int B, int slot) {
   flip_transpose_kernel<<<(64 * 64 * WS_K + 255) / 256, 256, 0, W->st>>>(p + W->poff[1], 64, 64, W->d_wt);
   scft_count_launches(2);
   WCK((conv<16, float, float, TA>(W->d_gb, 64, W->d_wt, nullptr, 64, 2, 0, a1, W->d_ga, B, W->st)));
-  // layer 0 (4 -> 64)
-  conv_wgrad_kernel<float><<<dim3(64, 4), 256, 0, W->st>>>(W->d_ga, W->d_feat, B, 4, 64, 1, g + W->poff[0], g + W->boff[0]);
+  // layer 0 (WS_IN -> 64)
+  conv_wgrad_kernel<float><<<dim3(64, WS_IN), 256, 0, W->st>>>(W->d_ga, W->d_feat, B, WS_IN, 64, 1, g + W->poff[0],
+                                                               g + W->boff[0]);
   scft_count_launches(1);
   WCK(cudaGetLastError());
   return SCFT_OK;

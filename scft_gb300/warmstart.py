@@ -18,7 +18,7 @@ from . import api
 from ._lib import check
 
 GRID = 256
-FEATURES = 4
+FEATURES = 5
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "warmstart_w0.npz")
 
 

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 def rand_inputs(B, seed=0):
     r = np.random.default_rng(seed)
-    f = r.uniform(-1, 1, (B, 4, 256)).astype(np.float32)
+    f = r.uniform(-1, 1, (B, 5, 256)).astype(np.float32)
     t = r.normal(0, 0.5, (B, 256)).astype(np.float32)
     return f, t
 
