@@ -13,7 +13,7 @@ device time, CUDA events on the library's stream); `e2e` repeats the
 measurement through the public C ABI with host buffers (batch creation from the
 caller's concatenated host arrays with its host-to-device copies, solve, and the
 device-to-host read of fields and densities inside the timed region).  On the
-warm-started batches, instances still running after update 34 race three forked
+warm-started batches, instances still running after update 42 race three forked
 mixing paths on idle thread groups (the outcome depends only on iteration
 counts); `value_without_forks` is the same measurement with forks off.
 
@@ -288,7 +288,7 @@ def ours_arm(args):
         sets.append([insts[i] for i in shard(insts, rank, world)])
     n_inst = sum(len(m) for m in sets) // len(sets)
     # forked paths for the noise-driven tail of the warm-started batch (3 paths
-    # from update 34 at an error <= 1e-5); off for the cold start, whose slow
+    # from update 42 at an error <= 1e-5); off for the cold start, whose slow
     # instances are slow for other reasons
     opts = api.solve_opts(precision=F32, tol=TOL, forks=0 if args.cold else 3)
     nofork = api.solve_opts(precision=F32, tol=TOL, forks=0)

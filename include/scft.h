@@ -156,7 +156,8 @@ typedef struct scft_instance {
 typedef struct scft_solve_opts {
   int precision;      /* SCFT_F32 (propagator in FP32, mixing/residual FP64) or SCFT_F64 */
   double tol;         /* ||phi - f0||_inf target */
-  double tol32_factor;/* FP32 iterations stop at tol * tol32_factor */
+  double tol32_factor;/* FP32 iterations stop at tol * tol32_factor (default 0.65: the FP32 density's
+                         bias, about 1.3e-7, keeps the field within tol under FP64) */
   int verify64;       /* FP32-converged instances are re-evaluated once in FP64 */
   int maxit;
   int depth;          /* Anderson history depth (<= 16) */

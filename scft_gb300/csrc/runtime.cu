@@ -1874,7 +1874,7 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   memset(o, 0, sizeof *o);
   o->precision = SCFT_F32;
   o->tol = 1e-6;
-  o->tol32_factor = 0.5;
+  o->tol32_factor = 0.65;
   o->verify64 = 0;
   o->maxit = 2000;
   o->depth = 10;
@@ -1894,7 +1894,7 @@ void scft_solve_opts_init(scft_solve_opts *o) {
   o->finish_tol = 1e-4;
   o->budget_ms = 0.0;
   o->forks = 0;
-  o->fork_at = 34;
+  o->fork_at = 42;
   o->fork_grace = 6;
   o->fork_first = 1;
   o->fork_err = 1e-5;

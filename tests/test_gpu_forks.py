@@ -43,7 +43,7 @@ def test_forks_never_cost_iterations_and_keep_the_instances_own_wins():
             np.testing.assert_array_equal(phi1[i], phi0[i])
         # the FP32 stopping tolerance on the density the winner reported, and the
         # full tolerance under the FP64 propagator at the winner's field
-        assert np.abs(phi1[i][1:-1] - d["f0"][1:-1]).max() <= 0.5e-6 * (1 + 1e-9), i
+        assert np.abs(phi1[i][1:-1] - d["f0"][1:-1]).max() <= 1e-6 * api.solve_opts().tol32_factor * (1 + 1e-9), i
         assert np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max() <= 1e-6, i
 
 

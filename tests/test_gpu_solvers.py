@@ -200,7 +200,7 @@ def test_fused_first_iterations_match_batchwide():
 
 def test_fused_solve_converges_like_batchwide():
     """Both forms converge every instance to the FP32 stopping tolerance
-    (0.5e-6) with matching mean iteration counts.  Single trajectories part
+    (tol x the default tol32_factor) with matching mean iteration counts.  Single trajectories part
     once the Anderson least squares amplifies the rounding differences of the
     reductions, so single counts are not compared."""
     insts = W.batch_mixed(96, seed=77)
@@ -215,7 +215,8 @@ def test_fused_solve_converges_like_batchwide():
         r, phi = out[fused]
         assert np.all(r["status"] & ST_CONVERGED), (fused, r["status"])
         for i, d in enumerate(insts):
-            bound = 1e-6 if r["status"][i] & 64 else 0.5e-6  # finished in FP64: full tolerance
+            # finished in FP64: full tolerance
+            bound = 1e-6 if r["status"][i] & 64 else 1e-6 * api.solve_opts().tol32_factor
             assert np.abs(phi[i][1:-1] - d["f0"][1:-1]).max() <= bound * (1 + 1e-9), (fused, i)
     i0, i1 = out[0][0]["iterations"], out[1][0]["iterations"]
     assert abs(i1.mean() - i0.mean()) <= 0.15 * i0.mean(), (i0.mean(), i1.mean())
