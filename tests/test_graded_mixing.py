@@ -148,3 +148,22 @@ def test_gpu_graded_fp64_hand_off_matches_the_oracle(oracle):
             assert r["status"][i] & ST_CONVERGED, (i, r["status"][i], r["iterations"][i])
         if r["status"][i] & ST_CONVERGED:
             assert np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max() <= tol, i
+
+
+@pytest.mark.gpu
+def test_gpu_staged_solve_on_a_mixed_batch_converges_every_instance():
+    """A staged solve of a uniform-mesh batch in which only some instances share
+    a mesh shape (node count, contour steps, rule): shapes with fewer than three
+    instances stay in the first stage, the rest transfer; every instance
+    converges to the FP32 stopping tolerance and passes 1e-6 under FP64."""
+    insts = [W.instance(m, 2.0 + 0.4 * k, ns, 7, k) for k, (m, ns) in
+             enumerate([(128, 1024)] * 9 + [(200, 2048)] * 2 + [(96, 512)] * 5)]
+    with api.Batch(insts) as b:
+        r = b.solve(api.solve_opts(precision=F32, tol=1e-6, transfer_stride=3))
+        st = b.status()
+        b.evaluate(F64)
+        _, phi64, _ = b.get()
+    assert np.all(r["status"] & ST_CONVERGED), r["status"]
+    np.testing.assert_array_equal(st, r["status"])
+    for i, d in enumerate(insts):
+        assert np.abs(phi64[i][1:-1] - d["f0"][1:-1]).max() <= 1e-6, i
