@@ -3,19 +3,25 @@
 // fields come from files: 1D_FEM.c:321-342, scft_util.cc:14-41).
 //
 // One CTA of 128 threads per instance.  For each tap k the layer is the GEMM
-//   D[p][co] += A_k[p][ci] * B_k[co][ci],   A_k[p][ci] = x[ci][p + (k-2) dil],
+//   D[p][co] += A_k[p][ci] * B_k[co][ci],   A_k[p][ci] = x[ci][p + s_k], s_k = (k-2) dil,
 // M = 256 points (two 128-row tiles), N = 64 output channels, K = 5 taps x 64
-// input channels.  The threads build the five shifted copies A_k (BF16) in
-// shared memory in the canonical K-major layout without swizzle (8-row x
-// 16-byte core matrices: K chunks 128 B apart, row groups 1024 B apart); the
-// BF16 weight image B (same layout) arrives by one bulk asynchronous copy
-// (cp.async.bulk, completion on an mbarrier).  One thread issues the 2 x 20
-// tcgen05.mma (kind::f16, BF16 x BF16 -> FP32) into two 64-column accumulators
-// in tensor memory and commits them to a second mbarrier; each warp then reads
-// its 32 rows of both accumulators (tcgen05.ld 32x32b), adds the bias, applies
-// tanh and stores BF16.  Every wait is bounded (one second of %globaltimer);
-// a wait that runs out sets *err, skips what depended on it and still frees the
-// tensor memory.
+// input channels.  A tensor-map copy (cp.async.bulk.tensor, TMA) brings the
+// instance's input x[64][256] (BF16, 32 KB) into shared memory, and one bulk
+// copy brings the BF16 weight image; both complete on mbarriers.  The threads
+// then transpose x into the canonical K-major operand layout without swizzle
+// (8-row x 16-byte core matrices: K chunks 128 B apart, row groups 1024 B
+// apart).  An operand's start must fall on a row group, so the shifts s_k are
+// served by 8/dil copies of the transposed input, copy i shifted by i*dil rows:
+// tap k reads copy (s_k mod 8)/dil from the row group that puts row p at
+// p + s_k.  One thread issues the 2 x 20 tcgen05.mma (kind::f16, BF16 x BF16
+// -> FP32) into two 64-column accumulators in tensor memory and commits them
+// to a third mbarrier; each warp then reads its 32 rows of both accumulators
+// (tcgen05.ld 32x32b), adds the bias, applies tanh and stores BF16.  Every wait
+// is bounded (one second of %globaltimer); a wait that runs out sets *err,
+// skips what depended on it and still frees the tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdint>
 
 #include "conv_tc.cuh"
@@ -24,15 +30,25 @@ namespace scft {
 namespace {
 
 constexpr int P = 256, CH = 64, KT = 5, THREADS = 128;
-constexpr int A_TAP = P * CH * 2;       // bytes of one shifted copy A_k (both row tiles)
-constexpr int A_TILE = 128 * CH * 2;    // bytes of one 128-row tile of A_k
-constexpr int A_BYTES = KT * A_TAP;
+constexpr int X_BYTES = CH * P * 2;     // the instance's input, [ci][p] BF16
 constexpr int B_TAP = CH * CH * 2;
 constexpr int B_BYTES = KT * B_TAP;
 static_assert(B_BYTES == CONV_TC_IMAGE_BYTES, "weight image size");
-constexpr int SMEM_BYTES = A_BYTES + B_BYTES + 64;  // + two mbarriers, the TMEM address, a flag
 constexpr unsigned TMEM_COLS = 128;                // two 128 x 64 FP32 accumulators
 constexpr unsigned long long WAIT_NS = 1000000000ull;
+
+// Shifted copies of the transposed input for dilation DIL (2, 4 or 8): NR
+// copies of R rows; copy i holds row j = x^T[j + i*DIL - H] (zero outside the
+// 256 points), H the halo rounded up to a row group.
+template <int DIL>
+struct Copies {
+  static_assert(DIL == 2 || DIL == 4 || DIL == 8, "dilation 2, 4 or 8");
+  static constexpr int NR = 8 / DIL;
+  static constexpr int H = (2 * DIL + 7) / 8 * 8;
+  static constexpr int R = P + 2 * H;
+  static constexpr int BYTES = NR * R * CH * 2;
+  static constexpr int SMEM = X_BYTES + BYTES + B_BYTES + 64;  // + three mbarriers, the TMEM address, a flag
+};
 
 // Byte offset of element (row r, K element e) in a canonical K-major tile
 // without swizzle.
@@ -93,18 +109,21 @@ __global__ void conv_tc_pack_kernel(const float *__restrict__ W, __nv_bfloat16 *
 
 template <int DIL, bool ACT>
 __global__ void __launch_bounds__(THREADS, 1)
-    conv_tc_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ img,
+    conv_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __nv_bfloat16 *__restrict__ img,
                    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ y, int *err) {
+  using Cp = Copies<DIL>;
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char *A = sm;
-  unsigned char *Bs = sm + A_BYTES;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + A_BYTES + B_BYTES);  // [0] weights, [1] products
-  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 2);
+  unsigned char *X = sm;                       // [ci][p], 512 B per channel
+  unsigned char *A = sm + X_BYTES;             // the shifted copies
+  unsigned char *Bs = A + Cp::BYTES;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(Bs + B_BYTES);  // [0] input, [1] weights, [2] products
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 3);
   int *go = reinterpret_cast<int *>(tmem_slot + 1);
   const int b = blockIdx.x, t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const unsigned bar_w = smem_addr(&bar[0]), bar_d = smem_addr(&bar[1]);
+  const unsigned bar_x = smem_addr(&bar[0]), bar_w = smem_addr(&bar[1]), bar_d = smem_addr(&bar[2]);
 
   if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_x) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_w) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_d) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -117,44 +136,56 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   __syncthreads();
   if (t == 0) {
-    // the weight image: one bulk copy, completion counted on bar_w
+    // the input tile (rows b*64 .. b*64+63 of the [B*64][256] tensor) by TMA,
+    // the weight image by one bulk copy
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_x), "r"(X_BYTES) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_addr(X)),
+        "l"(reinterpret_cast<uint64_t>(&xmap)), "r"(0), "r"(b * CH), "r"(bar_x)
+        : "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_w), "r"(B_BYTES) : "memory");
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
             smem_addr(Bs)),
         "l"(img), "r"(B_BYTES), "r"(bar_w)
         : "memory");
+    const int ok = mbar_wait(bar_x, 0) ? 1 : 0;
+    if (!ok) atomicExch(err, 3);
+    *go = ok;
   }
+  __syncthreads();
 
-  // the five shifted copies A_k (zero outside the 256 points)
-  const unsigned short *xb = reinterpret_cast<const unsigned short *>(x) + (size_t)b * CH * P;
+  if (*go) {
+    // the shifted copies, transposed into the operand layout; consecutive
+    // threads take consecutive rows (conflict-free reads and writes)
+    const unsigned short *xs = reinterpret_cast<const unsigned short *>(X);
 #pragma unroll 1
-  for (int half = 0; half < 2; half++) {
-    const int p = half * 128 + t;
+    for (int i = 0; i < Cp::NR; i++) {
+      unsigned char *Ci = A + i * (Cp::R * CH * 2);
 #pragma unroll 1
-    for (int k = 0; k < KT; k++) {
-      const int q = p + (k - 2) * DIL;
-      const bool in = q >= 0 && q < P;
-      unsigned char *At = A + k * A_TAP;
+      for (int j = t; j < Cp::R; j += THREADS) {
+        const int q = j + i * DIL - Cp::H;
+        const bool in = q >= 0 && q < P;
 #pragma unroll
-      for (int c = 0; c < CH / 8; c++) {
-        uint32_t v[4];
+        for (int c = 0; c < CH / 8; c++) {
+          uint32_t v[4] = {0u, 0u, 0u, 0u};
+          if (in) {
 #pragma unroll
-        for (int h = 0; h < 4; h++) {
-          const uint32_t lo = in ? __ldg(xb + (8 * c + 2 * h) * P + q) : 0u;
-          const uint32_t hi = in ? __ldg(xb + (8 * c + 2 * h + 1) * P + q) : 0u;
-          v[h] = lo | (hi << 16);
+            for (int h = 0; h < 4; h++)
+              v[h] = (uint32_t)xs[(8 * c + 2 * h) * P + q] | ((uint32_t)xs[(8 * c + 2 * h + 1) * P + q] << 16);
+          }
+          *reinterpret_cast<uint4 *>(Ci + canon(j, 8 * c)) = make_uint4(v[0], v[1], v[2], v[3]);
         }
-        *reinterpret_cast<uint4 *>(At + canon(p, 8 * c)) = make_uint4(v[0], v[1], v[2], v[3]);
       }
     }
+    // generic-proxy stores -> visible to the tensor core's reads
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  // generic-proxy stores -> visible to the tensor core's reads
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
   const unsigned tmem = *tmem_slot;
 
-  if (t == 0) {
+  if (t == 0 && *go) {
     int ok = mbar_wait(bar_w, 0) ? 1 : 0;
     if (ok) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -162,11 +193,14 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int m = 0; m < 2; m++) {
 #pragma unroll 1
         for (int k = 0; k < KT; k++) {
+          const int sft = (k - 2) * DIL, r = ((sft % 8) + 8) % 8, i = r / DIL;
+          const int row0 = m * 128 + sft - r + Cp::H;  // a multiple of 8
+          const unsigned char *Ak = A + i * (Cp::R * CH * 2) + (row0 / 8) * 1024;
 #pragma unroll
-          for (int j = 0; j < CH / 16; j++) {
-            const uint64_t ad = mdesc(smem_addr(A + k * A_TAP + m * A_TILE + j * 256));
-            const uint64_t bd = mdesc(smem_addr(Bs + k * B_TAP + j * 256));
-            const uint32_t acc = (k | j) ? 1u : 0u;
+          for (int jj = 0; jj < CH / 16; jj++) {
+            const uint64_t ad = mdesc(smem_addr(Ak + jj * 256));
+            const uint64_t bd = mdesc(smem_addr(Bs + k * B_TAP + jj * 256));
+            const uint32_t acc = (k | jj) ? 1u : 0u;
             asm volatile(
                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + m * 64),
@@ -197,12 +231,12 @@ __global__ void __launch_bounds__(THREADS, 1)
         __nv_bfloat16 *yp = y + (size_t)b * CH * P + p;
 #pragma unroll 1
         for (int c0 = 0; c0 < CH; c0 += 16) {
-          uint32_t r[16];
-          tmem_ld16(tmem + ((unsigned)(warp * 32) << 16) + m * 64 + c0, r);
+          uint32_t rr[16];
+          tmem_ld16(tmem + ((unsigned)(warp * 32) << 16) + m * 64 + c0, rr);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int i = 0; i < 16; i++) {
-            float v = __uint_as_float(r[i]) + __ldg(bias + c0 + i);
+            float v = __uint_as_float(rr[i]) + __ldg(bias + c0 + i);
             if (ACT) v = tanhf(v);
             yp[(size_t)(c0 + i) * P] = __float2bfloat16_rn(v);
           }
@@ -212,6 +246,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       atomicExch(err, 2);
       mbar_wait(bar_d, 0);  // give products still in flight a second chance before the memory goes
     }
+  } else if (t == 0) {
+    // copies issued but not waited for must land before the CTA's memory goes
+    mbar_wait(bar_x, 0);
+    mbar_wait(bar_w, 0);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -219,13 +257,41 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link to the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  }
+  return fn;
+}
+
 template <int DIL, bool ACT>
 cudaError_t launch(const __nv_bfloat16 *x, const __nv_bfloat16 *img, const float *bias, __nv_bfloat16 *y, int B,
                    int *err, cudaStream_t st) {
+  // x as a [B*64][256] BF16 tensor, one 64 x 256 box per instance
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  CUtensorMap map;
+  const cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)B * CH};
+  const cuuint64_t strides[1] = {(cuuint64_t)P * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)P, (cuuint32_t)CH};
+  const cuuint32_t estr[2] = {1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(x), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
   auto kern = conv_tc_kernel<DIL, ACT>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Copies<DIL>::SMEM);
   if (e != cudaSuccess) return e;
-  kern<<<B, THREADS, SMEM_BYTES, st>>>(x, img, bias, y, err);
+  kern<<<B, THREADS, Copies<DIL>::SMEM, st>>>(map, img, bias, y, err);
   return cudaGetLastError();
 }
 
@@ -240,8 +306,6 @@ cudaError_t conv_tc_forward(const __nv_bfloat16 *x, const __nv_bfloat16 *img, co
                             __nv_bfloat16 *y, int B, int *err, cudaStream_t st) {
   if (B <= 0) return cudaSuccess;
   switch (dil * 2 + (act ? 1 : 0)) {
-    case 2: return launch<1, false>(x, img, bias, y, B, err, st);
-    case 3: return launch<1, true>(x, img, bias, y, B, err, st);
     case 4: return launch<2, false>(x, img, bias, y, B, err, st);
     case 5: return launch<2, true>(x, img, bias, y, B, err, st);
     case 8: return launch<4, false>(x, img, bias, y, B, err, st);

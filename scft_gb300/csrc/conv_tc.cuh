@@ -14,7 +14,7 @@ constexpr int CONV_TC_IMAGE_BYTES = 5 * 64 * 64 * 2;
 cudaError_t conv_tc_pack(const float *W, __nv_bfloat16 *img, cudaStream_t st);
 
 // y[b][co][p] = act(bias[co] + sum_ci sum_k W[co][ci][k] x[b][ci][p + (k-2) dil]) for
-// B instances of 256 points, x and y BF16 [B][64][256], dil in {1, 2, 4, 8}, act = tanh
+// B instances of 256 points, x and y BF16 [B][64][256], dil in {2, 4, 8}, act = tanh
 // or identity.  Accumulation in FP32.  *err (device) receives a nonzero code if
 // a wait of the kernel ran out (the outputs of that instance are then not
 // written).
