@@ -57,9 +57,11 @@ def test_strerror_and_defaults_without_device():
     o = api.solve_opts()
     assert o.depth == 10 and o.beta == pytest.approx(1.0) and o.fused == 1 and o.precision == _lib.F32
     # forked paths off by default, with the bench's settings ready; graded-mesh step above ratio 16
-    assert o.forks == 0 and o.fork_at == 34 and o.fork_grace == 6 and o.fork_first == 1
+    assert o.forks == 0 and o.fork_at == 42 and o.fork_grace == 6 and o.fork_first == 1
     assert o.fork_err == pytest.approx(1e-5) and list(o.fork_scale)[:3] == pytest.approx([0.9, 0.8, 0.6])
     assert o.graded_ratio == pytest.approx(16.0) and o.precond_hfloor == pytest.approx(0.1)
+    # FP32 iterations stop at 0.65 tol; the staged solve is off
+    assert o.tol32_factor == pytest.approx(0.65) and o.transfer_stride == 0
     import ctypes as C
     c = _lib.ScftConfig()
     lib.scft_config_init(C.byref(c))
