@@ -310,6 +310,11 @@ static int plan(scft_batch *B, int p, double frac, int paths = 0) {
     const int CL = cluster_ctas(p == PREC_F64, c.C, c.NW);
     c.workers = (int)std::min((long long)c.items.size() * (1 + paths),
                               std::max(1LL, (long long)budget * c.gpc / CL));
+    // A class with a small share of the cost would otherwise get a handful of
+    // groups that run its instances one after another, a chain as long as the
+    // large classes' whole solve: one-CTA classes get at least one group per
+    // instance up to 64 (a few CTAs, nothing next to the large classes).
+    if (CL == 1) c.workers = std::max(c.workers, (int)std::min<size_t>(c.items.size(), 64));
     c.grid = (c.workers + c.gpc - 1) / c.gpc * CL;
     c.slot_elems = (long long)(maxhalf + 1) * 32 * c.NW * c.C;
     const size_t esz = (p == PREC_F32) ? 4 : 8;
