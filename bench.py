@@ -687,8 +687,9 @@ def config_legs(ws):
     # the graded workload solved: all 512 instances, FP32 stopping at the
     # tolerance itself (these meshes leave a discretisation floor near 5e-7 on
     # ||phi - f0||), graded-mesh step, staged: every 8th instance in order of L
-    # (and the widest) solved from the cold start, every other one from the field
-    # interpolated between its two nearest solved neighbours; every field then
+    # (and the widest) solved from the cold start, every other one, and every
+    # instance still unconverged, from the field interpolated between its two
+    # nearest converged neighbours in later rounds; every field then
     # checked under the FP64 propagator.  The plain FP64 form (cold start) and the
     # FP32 form from the cold start run on the first 38 instances, one wave of
     # 4-CTA clusters on 152 SMs.
@@ -716,7 +717,7 @@ def config_legs(ws):
     out["batch_graded_solve"] = {"workload": "512 instances: 8192 elements graded by 1.002 toward both walls, "
                                              "8192 steps, L ~ U[2, 12]; FP32 stop at 1e-6, maxit 800, batch-wide "
                                              "form with the 4-CTA cluster propagator",
-                                 "instances": len(full), "start": "transferred (stride 8)", "ms": ms,
+                                 "instances": len(full), "start": "transferred (stride 8, rounds capped at 400/200/800)", "ms": ms,
                                  "converged": conv, "value": value, "unit": UNIT,
                                  "converged_first_38": int(ok[:wave].sum()),
                                  "iterations_mean": float(r["iterations"].mean()),

@@ -214,13 +214,16 @@ typedef struct scft_solve_opts {
                             mesh graded to 1e-6 would otherwise throttle every other node) */
   double precond_hfloor;
   int transfer_stride;/* > 1: instances that share a mesh shape (node count, contour steps, rule and
-                         spacing ratio) are solved in two stages.  Sorted by film width L, every
+                         spacing ratio) are solved in rounds.  Sorted by film width L, every
                          transfer_stride-th of them (and the widest) is solved first from its own
-                         field; each other one then starts from the field interpolated in L, node by
-                         node, between its two nearest converged first-stage neighbours, and is
-                         solved.  On meshes graded toward the walls, where the field's wall layer
-                         makes any smooth start slower than the cold one, a neighbour's converged
-                         field is a start within a few iterations of the answer.  0 or 1: off */
+                         field with the cap maxit/2; then every instance not converged starts from
+                         the field interpolated in L, node by node, between its two nearest
+                         converged neighbours, and is solved with the cap maxit/4, and once more
+                         with the full cap for those still not converged.  Iteration counts add up
+                         over an instance's rounds.  On meshes graded toward the walls, where the
+                         field's wall layer makes any smooth start slower than the cold one, a
+                         neighbour's converged field is a start within a few iterations of the
+                         answer.  0 or 1: off */
 } scft_solve_opts;
 
 typedef struct scft_result {

@@ -1100,103 +1100,113 @@ static int solve(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
 }
 
 // Staged solve (transfer_stride > 1).  Instances that share a mesh shape (node
-// count, contour steps, rule and spacing ratio to 1 %) are sorted by film width;
-// every stride-th of them and the widest are solved first, each from its own
-// field.  Every other one then starts from the field interpolated in the width,
-// node by node, between its nearest converged first-stage neighbours below and
-// above (one of them when only one converged; its own field when neither did),
-// and the second stage solves those.  Groups of fewer than three instances are
-// solved in the first stage.
+// count, contour steps, rule and spacing ratio to 1 %) are sorted by film width.
+// Round 0 solves every stride-th of them and the widest, each from its own
+// field, with the iteration cap maxit/2.  Each later round takes every instance
+// not converged so far (first-round failures included), starts it from the
+// field interpolated in the width, node by node, between its nearest converged
+// neighbours below and above (one of them when there is only one; its own field
+// when there is none), and solves those: round 1 with the cap maxit/4, round 2
+// with the full cap.  A converged neighbour of round 0 is a few tenths of L
+// away, one of round 1 a few hundredths, so a straggler of round 1 gets a closer
+// start in round 2.  Groups of fewer than three instances are solved in round 0.
 static int solve_staged(scft_batch *B, const scft_solve_opts *o, scft_result *res) {
   const int c = B->count, stride = o->transfer_stride;
   std::map<std::tuple<int, int, int, long>, std::vector<int>> groups;
   for (int i = 0; i < c; i++)
     groups[{B->n[i], B->nsteps[i], B->rule[i], std::lround(std::log(B->spacing_ratio[i]) * 100.0)}].push_back(i);
-  std::vector<int> first(c, 1), below(c, -1), above(c, -1);
+  std::vector<int> sel(c, 1);
+  std::vector<const std::vector<int> *> group_of(c, nullptr);
   for (auto &kv : groups) {
     auto &g = kv.second;
-    if (g.size() < 3) continue;
     std::stable_sort(g.begin(), g.end(), [&](int a, int b) { return B->width[a] < B->width[b]; });
+    for (int i : g) group_of[i] = &g;
+    if (g.size() < 3) continue;
     const int m = (int)g.size();
-    for (int r = 0; r < m; r++) first[g[r]] = (r % stride == 0 || r == m - 1) ? 1 : 0;
-    int last = -1;
-    for (int r = 0; r < m; r++) {
-      if (first[g[r]]) last = g[r];
-      else below[g[r]] = last;
-    }
-    last = -1;
-    for (int r = m - 1; r >= 0; r--) {
-      if (first[g[r]]) last = g[r];
-      else above[g[r]] = last;
-    }
+    for (int r = 0; r < m; r++) sel[g[r]] = (r % stride == 0 || r == m - 1) ? 1 : 0;
   }
   if (!B->d_select) {
     int rc = dalloc(&B->d_select, (size_t)c);
     if (rc) return rc;
   }
-  std::vector<scft_result> r1(c), r2(c);
-  auto run_stage = [&](const std::vector<int> &sel, std::vector<scft_result> &out, float *ms) -> int {
+  std::vector<scft_result> out(c), rr(c);
+  std::vector<int> done(c, 0), its(c, 0);
+  float total_ms = 0.f;
+  const int caps[3] = {std::max(1, o->maxit / 2), std::max(1, o->maxit / 4), o->maxit};
+  for (int round = 0; round < 3; round++) {
+    if (round > 0) {
+      // this round's instances: every one not converged; their starts
+      std::vector<int> tplan;
+      std::vector<double> tt;
+      for (int i = 0; i < c; i++) {
+        sel[i] = done[i] ? 0 : 1;
+        if (done[i]) continue;
+        const std::vector<int> &g = *group_of[i];
+        int a = -1, b = -1;  // nearest converged neighbours below and above
+        for (int j : g) {
+          if (j == i || !done[j]) continue;
+          if (B->width[j] <= B->width[i] && (a < 0 || B->width[j] >= B->width[a])) a = j;
+          if (B->width[j] >= B->width[i] && (b < 0 || B->width[j] < B->width[b])) b = j;
+        }
+        if (a < 0 && b < 0) continue;
+        if (a < 0) a = b;
+        if (b < 0) b = a;
+        const double span = B->width[b] - B->width[a];
+        double t = span > 0.0 ? (B->width[i] - B->width[a]) / span : 0.0;
+        t = std::min(1.0, std::max(0.0, t));
+        tplan.insert(tplan.end(), {i, a, b, 0});
+        tt.push_back(t);
+      }
+      if (std::none_of(sel.begin(), sel.end(), [](int v) { return v != 0; })) break;
+      if (!tt.empty()) {
+        const int m = (int)tt.size();
+        int *d_plan = nullptr;
+        double *d_t = nullptr;
+        int rc;
+        if ((rc = dalloc(&d_plan, tplan.size())) || (rc = dalloc(&d_t, tt.size()))) {
+          dfree(d_plan);
+          return rc;
+        }
+        float msx = 0.f;
+        CK(cudaMemcpyAsync(d_plan, tplan.data(), tplan.size() * sizeof(int), cudaMemcpyHostToDevice, B->st));
+        CK(cudaMemcpyAsync(d_t, tt.data(), tt.size() * sizeof(double), cudaMemcpyHostToDevice, B->st));
+        CK(cudaEventRecord(B->t0, B->st));
+        transfer_kernel<<<m, 256, 0, B->st>>>(d_plan, d_t, m, B->d_n, B->d_node_off, B->d_w);
+        g_launches++;
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(B->t1, B->st));
+        CK(cudaEventSynchronize(B->t1));
+        CK(cudaEventElapsedTime(&msx, B->t0, B->t1));
+        total_ms += msx;
+        dfree(d_plan);
+        dfree(d_t);
+      }
+    }
     CK(cudaMemcpy(B->d_select, sel.data(), c * sizeof(int), cudaMemcpyHostToDevice));
     B->use_select = true;
     scft_solve_opts os = *o;
     os.transfer_stride = 0;
-    const int rc = solve(B, &os, out.data());
+    os.maxit = caps[round];
+    const int rc = solve(B, &os, rr.data());
     B->use_select = false;
-    *ms = B->last_ms;
-    return rc;
-  };
-  float ms1 = 0.f, ms2 = 0.f, msx = 0.f;
-  int rc = run_stage(first, r1, &ms1);
-  if (rc) return rc;
-  // second-stage starts from the converged first-stage neighbours
-  std::vector<int> second(c, 0), tplan;
-  std::vector<double> tt;
-  for (int i = 0; i < c; i++) {
-    if (first[i]) continue;
-    second[i] = 1;
-    int a = below[i], b = above[i];
-    const bool ca = a >= 0 && (r1[a].status & SCFT_ST_CONVERGED), cb = b >= 0 && (r1[b].status & SCFT_ST_CONVERGED);
-    if (!ca && !cb) continue;
-    if (!ca) a = b;
-    if (!cb) b = a;
-    const double span = B->width[b] - B->width[a];
-    double t = span > 0.0 ? (B->width[i] - B->width[a]) / span : 0.0;
-    t = std::min(1.0, std::max(0.0, t));
-    tplan.insert(tplan.end(), {i, a, b, 0});
-    tt.push_back(t);
-  }
-  if (!tt.empty()) {
-    const int m = (int)tt.size();
-    int *d_plan = nullptr;
-    double *d_t = nullptr;
-    if ((rc = dalloc(&d_plan, tplan.size())) || (rc = dalloc(&d_t, tt.size()))) {
-      dfree(d_plan);
-      return rc;
+    if (rc) return rc;
+    total_ms += B->last_ms;
+    for (int i = 0; i < c; i++) {
+      if (!sel[i]) continue;
+      out[i] = rr[i];
+      its[i] += rr[i].iterations;
+      out[i].iterations = its[i];  // every round's updates of the instance
+      if (rr[i].status & SCFT_ST_CONVERGED) done[i] = 1;
     }
-    CK(cudaMemcpyAsync(d_plan, tplan.data(), tplan.size() * sizeof(int), cudaMemcpyHostToDevice, B->st));
-    CK(cudaMemcpyAsync(d_t, tt.data(), tt.size() * sizeof(double), cudaMemcpyHostToDevice, B->st));
-    CK(cudaEventRecord(B->t0, B->st));
-    transfer_kernel<<<m, 256, 0, B->st>>>(d_plan, d_t, m, B->d_n, B->d_node_off, B->d_w);
-    g_launches++;
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(B->t1, B->st));
-    CK(cudaEventSynchronize(B->t1));
-    CK(cudaEventElapsedTime(&msx, B->t0, B->t1));
-    dfree(d_plan);
-    dfree(d_t);
   }
-  if (std::any_of(second.begin(), second.end(), [](int v) { return v != 0; })) {
-    if ((rc = run_stage(second, r2, &ms2))) return rc;
-  }
-  // merged outcome: each instance from its own stage
+  // the outcome of each instance's last round, with the updates of all its rounds
   std::vector<int> st(c);
   for (int i = 0; i < c; i++) {
-    const scft_result &r = first[i] ? r1[i] : r2[i];
-    st[i] = r.status;
-    if (res) res[i] = r;
+    st[i] = out[i].status;
+    if (res) res[i] = out[i];
   }
   CK(cudaMemcpy(B->d_status, st.data(), c * sizeof(int), cudaMemcpyHostToDevice));
-  B->last_ms = ms1 + msx + ms2;
+  B->last_ms = total_ms;
   return SCFT_OK;
 }
 
