@@ -502,12 +502,20 @@ def ours_arm(args):
         if args.detail:
             with open(args.detail, "w") as f:
                 f.write(txt + "\n")
-        print(json.dumps(compact(line)), flush=True)
+        # the contract's keys first, the comparison figures (other forms, configs)
+        # last, so that a reader of the line's last 1.5 KB sees all of them
+        first = [k for k in LINE_KEYS if k in line]
+        ordered = {k: line[k] for k in first + [k for k in line if k not in first]}
+        print(json.dumps(compact(ordered)), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
+# the graded workload's staged solve: stride and mixing (chosen on seed 6)
+GRADED_STRIDE, GRADED_DEPTH, GRADED_PRECOND, GRADED_TOL32 = 16, 16, 0.2, 0.95
+LINE_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+             "vs_baseline", "dtype", "data", "config", "gpu_launches", "clocks", "roofline", "e2e", "cpu_baseline")
 CPU_MIXING = "or_anderson_solve (the GPU's Anderson mixing in C; adm_chen diverges from these cold starts)"
 
 
@@ -684,17 +692,20 @@ def config_legs(ws):
                                 "alg_GBps_fp32": alg / (ms32 / 1e3) / 1e9, "frac_of_peak": alg / (ms32 / 1e3) / 1e9 / peak,
                                 "peak_source": kind}
 
-    # the graded workload solved: all 512 instances, FP32 stopping at the
-    # tolerance itself (these meshes leave a discretisation floor near 5e-7 on
-    # ||phi - f0||), graded-mesh step, staged: every 8th instance in order of L
+    # the graded workload solved: all 512 instances, FP32 stopping at 0.95 of the
+    # tolerance (these meshes leave a discretisation floor of 5e-7 to 1.5e-6 on
+    # ||phi - f0||), graded-mesh step, staged: every 16th instance in order of L
     # (and the widest) solved from the cold start, every other one, and every
     # instance still unconverged, from the field interpolated between its two
-    # nearest converged neighbours in later rounds; every field then
-    # checked under the FP64 propagator.  The plain FP64 form (cold start) and the
-    # FP32 form from the cold start run on the first 38 instances, one wave of
-    # 4-CTA clusters on 152 SMs.
+    # nearest converged neighbours in later rounds; every field then checked
+    # under the FP64 propagator.  Mixing for these meshes: Anderson depth 16,
+    # preconditioner 0.2; stride, mixing and the FP32 stop chosen on the 512
+    # instances of seed 6 (this workload is seed 5).  The plain FP64 form (cold start) and the FP32 form from the cold
+    # start run on the first 38 instances, one wave of 4-CTA clusters on 152 SMs,
+    # with the same mixing.
     full = W.batch_graded(512)
-    o = api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=800, transfer_stride=8)
+    mix = dict(tol=TOL, maxit=800, depth=GRADED_DEPTH, precond=GRADED_PRECOND)
+    o = api.solve_opts(precision=F32, tol32_factor=GRADED_TOL32, transfer_stride=GRADED_STRIDE, **mix)
     with api.Batch(full) as b:
         r = b.solve(o)
         ms = b.last_ms()
@@ -705,8 +716,8 @@ def config_legs(ws):
     wave = 38
     forms = {}
     with api.Batch(full[:wave]) as b:
-        for name, ow in (("plain_fp64_cold", api.solve_opts(precision=F64, tol=TOL, maxit=800)),
-                         ("fp32_cold", api.solve_opts(precision=F32, tol=TOL, tol32_factor=1.0, maxit=800))):
+        for name, ow in (("plain_fp64_cold", api.solve_opts(precision=F64, **mix)),
+                         ("fp32_cold", api.solve_opts(precision=F32, tol32_factor=GRADED_TOL32, **mix))):
             b.reset()
             rw = b.solve(ow)
             cw = int(((rw["status"] & ST_CONVERGED) != 0).sum())
@@ -715,9 +726,9 @@ def config_legs(ws):
     conv = int(ok.sum())
     value = conv / (ms / 1e3)
     out["batch_graded_solve"] = {"workload": "512 instances: 8192 elements graded by 1.002 toward both walls, "
-                                             "8192 steps, L ~ U[2, 12]; FP32 stop at 1e-6, maxit 800, batch-wide "
-                                             "form with the 4-CTA cluster propagator",
-                                 "instances": len(full), "start": "transferred (stride 8, rounds capped at 400/200/800)", "ms": ms,
+                                             "8192 steps, L ~ U[2, 12]; FP32 stop at 0.95e-6, maxit 800, Anderson depth 16, "
+                                             "preconditioner 0.2, batch-wide form with the 4-CTA cluster propagator",
+                                 "instances": len(full), "start": f"transferred (stride {GRADED_STRIDE}, rounds)", "ms": ms,
                                  "converged": conv, "value": value, "unit": UNIT,
                                  "converged_first_38": int(ok[:wave].sum()),
                                  "iterations_mean": float(r["iterations"].mean()),

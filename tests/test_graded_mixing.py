@@ -55,6 +55,23 @@ def test_gpu_graded_iterates_match_oracle(oracle, k):
 
 
 @pytest.mark.gpu
+def test_gpu_graded_iterates_match_oracle_at_depth_16(oracle):
+    """20 FP64 iterations with the mixing used for graded batches (Anderson depth
+    16, preconditioner 0.2), so that the history fills beyond the default depth,
+    against the oracle with the same options."""
+    k, mix = 20, dict(depth=16, precond=0.2)
+    insts = [graded(i) for i in range(3)]
+    with api.Batch(insts) as b:
+        b.solve(precision=F64, tol=1e-12, maxit=k, **mix)
+        w, _, _ = b.get()
+    for i, d in enumerate(insts):
+        p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"])
+        rc, wo, it, err = oracle.anderson_solve(p, d["w0"], tol=1e-12, maxit=k, **mix)
+        assert it == k
+        np.testing.assert_allclose(w[i], wo, rtol=0, atol=1e-6 * max(1.0, np.abs(wo).max()))
+
+
+@pytest.mark.gpu
 def test_gpu_graded_batch_converges():
     """A batch of graded instances converges in the fused FP32 solve, and every
     field passes the tolerance under the FP64 propagator.  These 512-element
