@@ -56,10 +56,15 @@ def test_gpu_graded_iterates_match_oracle(oracle, k):
 
 @pytest.mark.gpu
 def test_gpu_graded_iterates_match_oracle_at_depth_16(oracle):
-    """20 FP64 iterations with the mixing used for graded batches (Anderson depth
-    16, preconditioner 0.2), so that the history fills beyond the default depth,
-    against the oracle with the same options."""
-    k, mix = 20, dict(depth=16, precond=0.2)
+    """13 FP64 iterations with the mixing used for graded batches (Anderson depth
+    16, preconditioner 0.2), so that the history holds more than the default 10
+    entries, against the oracle with the same options.  From a cold start these
+    iterations amplify rounding (clamped wall nodes, near-singular least
+    squares): the oracle's own 13th iterate moves by up to 5e-5 of max|w| when
+    its start moves by 1e-14.  The bound is 20 times that spread, measured here
+    for each instance; the depth-10 iterate differs from the depth-16 one by more
+    than 0.1 of max|w|, far outside it."""
+    k, mix = 13, dict(depth=16, precond=0.2)
     insts = [graded(i) for i in range(3)]
     with api.Batch(insts) as b:
         b.solve(precision=F64, tol=1e-12, maxit=k, **mix)
@@ -68,7 +73,17 @@ def test_gpu_graded_iterates_match_oracle_at_depth_16(oracle):
         p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"])
         rc, wo, it, err = oracle.anderson_solve(p, d["w0"], tol=1e-12, maxit=k, **mix)
         assert it == k
-        np.testing.assert_allclose(w[i], wo, rtol=0, atol=1e-6 * max(1.0, np.abs(wo).max()))
+        scale = max(1.0, np.abs(wo).max())
+        spread = 0.0
+        for e in (1e-14, -1e-14):
+            w1 = d["w0"].copy()
+            w1[1:-1] *= 1.0 + e
+            spread = max(spread, np.abs(oracle.anderson_solve(p, w1, tol=1e-12, maxit=k, **mix)[1] - wo).max())
+        bound = max(1e-8 * scale, 20.0 * spread)
+        assert bound <= 1e-3 * scale, (i, spread / scale)
+        np.testing.assert_allclose(w[i], wo, rtol=0, atol=bound)
+        w10 = oracle.anderson_solve(p, d["w0"], tol=1e-12, maxit=k, depth=10, precond=0.2)[1]
+        assert np.abs(w10 - wo).max() > 100.0 * bound, i
 
 
 @pytest.mark.gpu
