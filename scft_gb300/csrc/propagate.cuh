@@ -52,6 +52,19 @@ namespace scft {
 #define FORK_WAIT_NS 30000000000ull
 #endif
 
+// The second half of a contour pass reads back the slices the first half
+// stored, one step ahead into registers.  Under load the slices come from HBM
+// at a latency longer than a step, so each step of the packed FP32 loop in
+// one-CTA groups also asks L2 for the slice it will read PREFETCH_STEPS steps
+// later (prefetch.global.L2: no register).  Measured on the GB300: the
+// warm-start evaluation classes' passes 7-13 % shorter; the cluster classes
+// (graded meshes, barrier-bound) 7 % longer, so they do without; no change for
+// the FP64 batch.
+#ifndef PREFETCH_STEPS
+#define PREFETCH_STEPS 4
+#endif
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Minimum resident CTAs per SM the fused solve kernel is compiled for (its
 // register budget); the planner sizes its grid from the occupancy it gets.
 #ifndef SOLVE_MIN_CTAS
@@ -432,6 +445,12 @@ struct Propagator {
       float2 pre2[H];
 #pragma unroll
       for (int i = 0; i < H; i++) pre2[i] = nxt2[i];
+      if (CL == 1 && k + PREFETCH_STEPS < ns) {
+        const float2 *pf = slot2 + (long long)(ns - k - 1 - PREFETCH_STEPS) * H * T + P;
+#pragma unroll
+        for (int i = 0; i < H; i++)
+          if (live(i)) prefetch_l2(pf + (long long)i * T);
+      }
       if (k < ns) {
         const float2 *src = slot2 + (long long)(ns - k - 1) * H * T + P;
 #pragma unroll
