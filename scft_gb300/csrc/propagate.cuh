@@ -14,7 +14,9 @@
 //                 shuffles, lane 31 is the warp separator;
 //   group level : the NW warp separators form a tridiagonal system solved
 //                 redundantly by every warp (PCR with shuffles); two named
-//                 barriers per step exchange the warp-boundary values.
+//                 barriers per step exchange the warp-boundary values (on
+//                 thread-block clusters: one CTA barrier and st.async stores
+//                 completing on mbarriers, see cx_*).
 //
 // The density phi_i = sum_k W_k q_k,i q_{nsteps-k},i (romint.c:21-57 Romberg
 // weights, or the trapezoid of simple_FEM_1D_transient.m:119-124) is accumulated
@@ -104,7 +106,72 @@ struct GroupSmem {
   int ired[NW];
   R qw[16];
   int item;
+  // Cluster classes only: the per-step exchange between the CTAs of a cluster
+  // (see cx_* below).  x_next: the next CTA's first warp's (zc0, zw); x_R: every
+  // warp's level-2 right-hand side, double-buffered by step parity; xbar: the
+  // mbarriers their remote stores complete on (x_next, x_R parity 0, parity 1).
+  R x_next[2];
+  R x_R[2][NW];
+  unsigned long long xbar[3];
+  unsigned xk;  // exchange steps taken by this CTA (all instances so far)
+  int xfail;    // a bounded exchange wait ran out (the cluster's results are void)
 };
+
+// Per-step exchange of the cluster classes.  Instead of two cluster barriers
+// per contour step (each a release/acquire of the distributed-shared-memory
+// stores by all CTAs), values move by st.async into the consumer CTA's shared
+// memory and complete on an mbarrier there (transaction bytes), so a consumer
+// waits only for the bytes it reads:
+//   * (zc0, zw) of a warp go to the previous warp: within a CTA through shared
+//     memory and one CTA barrier, across CTAs (first warp of CTA r to the last
+//     warp of CTA r - 1) by st.async on x_next / xbar[0];
+//   * each warp's level-2 right-hand side goes to every CTA's x_R[parity] /
+//     xbar[1 + parity].
+// Ordering: a warp sends step k+1's values only after the step-k exchange of
+// its own CTA completed, which needs every warp's step-k right-hand side, which
+// each warp produces after reading its step-k inputs; so x_next and its
+// mbarrier need one buffer, while x_R, written by warps of other CTAs that may
+// be one step ahead of a reader, needs two.  Each phase is armed (expected
+// bytes) by one thread of the consumer CTA after it saw the previous phase
+// complete; bytes that arrive before the arming count toward the armed phase.
+// Every wait is bounded: after CX_WAIT_NS the thread marks every CTA of the
+// cluster failed, and from then on the CTAs skip the exchange (no send, no
+// wait, no arming), finish the same steps and report ST_WATCHDOG.
+#ifndef CX_WAIT_NS
+#define CX_WAIT_NS 1000000000ull
+#endif
+__device__ __forceinline__ unsigned cx_smem(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned cx_remote(unsigned a, int rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cx_init(unsigned bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void cx_arm(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool cx_test(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void cx_send(unsigned raddr, float v, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(raddr),
+               "r"(__float_as_uint(v)), "r"(rbar)
+               : "memory");
+}
+__device__ __forceinline__ void cx_send(unsigned raddr, double v, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(raddr),
+               "l"(__double_as_longlong(v)), "r"(rbar)
+               : "memory");
+}
 
 template <int NW>
 struct Log2 { static constexpr int v = NW <= 1 ? 0 : 1 + Log2<NW / 2>::v; };
@@ -665,6 +732,33 @@ struct Propagator {
     const R r_dls = (R)dls, r_dus = (R)dus, r_vcn = (R)vcn, r_wcn = (R)wcn;
     const bool last_chunk = (P == T - 1);
 
+    // Cluster classes: this CTA's rank in the cluster, the warp's index within
+    // the CTA, the exchange steps taken so far and whether the exchange failed.
+    constexpr int WPC = NW / CL;  // warps per CTA
+    const int xrank = P / CTA, xwl = wid % WPC;
+    unsigned xk = 0;
+    bool xbad = false;
+    if constexpr (CL > 1) {
+      xk = S.xk;
+      xbad = S.xfail != 0;
+    }
+    // Bounded wait for phase `parity` of one of this CTA's exchange mbarriers.
+    auto xwait = [&](unsigned bar, unsigned parity) {
+      if (xbad || cx_test(bar, parity)) return;
+      const unsigned long long t0 = global_ns();
+      for (;;) {
+        if (*(volatile int *)&S.xfail) { xbad = true; return; }
+        if (cx_test(bar, parity)) return;
+        if (global_ns() - t0 > CX_WAIT_NS) {
+          xbad = true;
+          for (int r = 0; r < CL; r++)
+            asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cx_remote(cx_smem(&S.xfail), r)), "r"(1)
+                         : "memory");
+          return;
+        }
+      }
+    };
+
     // Separator solve of one contour step.  In: this thread's chunk-local z at
     // its first and last interior unknowns and the right-hand side at its
     // separator (C == 1: the right-hand side).  Out: the next chunk's z at its
@@ -690,20 +784,63 @@ struct Propagator {
         const R zw = t * ibw;
         const R zw30 = __shfl_sync(FULL, zw, 30);
         R zwn = (R)0;
-        if (lane == 0) { put(S.pub_zc0[wid], zc0); put(S.pub_zw[wid], zw); }
-        gsync(bar_id);
-        if (lane == 31) {
-          const bool has_next = (wid + 1 < NW);
-          const R zcx = has_next ? S.pub_zc0[wid + 1] : (R)0;
-          zwn = has_next ? S.pub_zw[wid + 1] : (R)0;
-          if (C > 1) {
-            zc0n = zcx;
-            rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zcl, rl));
+        R t2;
+        if constexpr (CL > 1) {
+          const unsigned par = xk & 1u;
+          if (lane == 0) {
+            S.pub_zc0[wid] = zc0;
+            S.pub_zw[wid] = zw;
+            if (xwl == 0 && xrank > 0 && !xbad) {  // to the last warp of the previous CTA
+              const unsigned rb = cx_remote(cx_smem(&S.xbar[0]), xrank - 1);
+              cx_send(cx_remote(cx_smem(&S.x_next[0]), xrank - 1), zc0, rb);
+              cx_send(cx_remote(cx_smem(&S.x_next[1]), xrank - 1), zw, rb);
+            }
           }
-          put(S.pub_R[wid], fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho)));
+          group_sync(bar_id, CTA);
+          if (lane == 31) {
+            R zcx = (R)0;
+            if (wid + 1 < NW) {
+              if (xwl + 1 < WPC) {
+                zcx = S.pub_zc0[wid + 1];
+                zwn = S.pub_zw[wid + 1];
+              } else {
+                xwait(cx_smem(&S.xbar[0]), par);
+                if (!xbad) cx_arm(cx_smem(&S.xbar[0]), 2 * sizeof(R));
+                zcx = S.x_next[0];
+                zwn = S.x_next[1];
+              }
+            }
+            if (C > 1) {
+              zc0n = zcx;
+              rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zcl, rl));
+            }
+            const R rw = fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho));
+            if (!xbad) {
+#pragma unroll
+              for (int r = 0; r < CL; r++)
+                cx_send(cx_remote(cx_smem(&S.x_R[par][wid]), r), rw, cx_remote(cx_smem(&S.xbar[1 + par]), r));
+            }
+          }
+          xwait(cx_smem(&S.xbar[1 + par]), (xk >> 1) & 1u);
+          if (threadIdx.x == 0 && !xbad) cx_arm(cx_smem(&S.xbar[1 + par]), NW * sizeof(R));
+          t2 = (lane < NW) ? S.x_R[par][lane] : (R)0;
+          xk++;
+        } else {
+          if (lane == 0) { put(S.pub_zc0[wid], zc0); put(S.pub_zw[wid], zw); }
+          gsync(bar_id);
+          if (lane == 31) {
+            const bool has_next = (wid + 1 < NW);
+            const R zcx = has_next ? S.pub_zc0[wid + 1] : (R)0;
+            zwn = has_next ? S.pub_zw[wid + 1] : (R)0;
+            if (C > 1) {
+              zc0n = zcx;
+              rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zcl, rl));
+            }
+            put(S.pub_R[wid], fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho)));
+          }
+          gsync(bar_id);
+          t2 = (lane < NW) ? S.pub_R[lane] : (R)0;
         }
-        gsync(bar_id);
-        R t2 = (lane < NW) ? S.pub_R[lane] : (R)0;
 #pragma unroll
         for (int l = 0; l < L2; l++) {
           const int s = 1 << l;
@@ -862,6 +999,10 @@ struct Propagator {
       }
     }
     if (P == 0) { phi[0] = 0.0; phi[n - 1] = 0.0; }
+    if constexpr (CL > 1) {
+      if (xbad) bad |= ST_WATCHDOG;  // an exchange wait ran out: this pass is void
+      if (threadIdx.x == 0) S.xk = xk;
+    }
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) {
       qpart += __shfl_down_sync(FULL, qpart, s);
@@ -905,6 +1046,18 @@ __global__ void __launch_bounds__(32 * NW / CL, 1) propagate_cluster_kernel(Batc
   const int P = rank * Pp::CTA + (int)threadIdx.x;
   const int worker = (int)(blockIdx.x / CL);
   if (worker >= cls.workers) return;  // the same for every CTA of the cluster
+  if (threadIdx.x == 0) {
+    sm.xk = 0;
+    sm.xfail = 0;
+    for (int i = 0; i < 3; i++) cx_init(cx_smem(&sm.xbar[i]));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // first phases: the next CTA's (zc0, zw) (not on the last CTA, which has
+    // no next), every warp's right-hand side for each step parity
+    if (rank + 1 < CL) cx_arm(cx_smem(&sm.xbar[0]), 2 * sizeof(R));
+    cx_arm(cx_smem(&sm.xbar[1]), NW * sizeof(R));
+    cx_arm(cx_smem(&sm.xbar[2]), NW * sizeof(R));
+  }
+  cooperative_groups::this_cluster().sync();  // barriers initialised before any remote store
   Pp::run(b, cls, sm, P, worker, 1);
 }
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as orc
-from scft_gb300 import F32, F64, RULE_ROMBERG, RULE_TRAPEZOID, ScftError, _lib, api, workloads as W
+from scft_gb300 import F32, F64, RULE_ROMBERG, RULE_TRAPEZOID, ST_WATCHDOG, ScftError, _lib, api, workloads as W
 
 pytestmark = pytest.mark.gpu
 
@@ -28,6 +28,7 @@ def test_largest_instance_matches_oracle_and_one_more_node_is_rejected(oracle):
             _, phi, Q = b.get()
             assert rel(phi[0], phi_ref) <= tol, (prec, rel(phi[0], phi_ref))
             assert abs(Q[0] - q_ref) <= tol * abs(q_ref)
+            assert (b.status()[0] & ST_WATCHDOG) == 0
     big = W.instance(8194, 12.0, 64, 3, 0)
     with api.Batch([big]) as b:
         with pytest.raises(ScftError) as e:
@@ -61,5 +62,32 @@ def test_single_interior_node_and_ragged_step_counts(oracle):
             for i, d in enumerate(insts):
                 p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d["rule"])
                 phi_ref, q_ref = oracle.propagate(p, d["w0"])
+                assert rel(phi[i], phi_ref) <= tol, (prec, i, rel(phi[i], phi_ref))
+                assert abs(Q[i] - q_ref) <= tol * abs(q_ref), (prec, i)
+
+
+def test_cluster_exchange_over_many_instances_per_cluster(oracle):
+    """Shapes above 2048 interior unknowns run on thread-block clusters whose
+    CTAs exchange each contour step's separator values by st.async stores that
+    complete on mbarriers, the barriers' phases carried from one instance to
+    the next.  200 such instances (more than the clusters resident at once, so
+    each cluster takes several) with odd and even step counts, in FP32 and FP64,
+    against the oracle; no exchange wait ran out.  A value that missed an
+    exchange would be a step stale (an error of order ds); the FP64 bound is
+    2e-10 because on these 3000-element meshes with about 60 steps the FP64
+    propagator's rounding differs from the oracle's Thomas sweeps by up to
+    1.05e-10 of max(phi)."""
+    insts = [W.instance(3000 + 7 * (k % 5), 4.0 + 0.01 * k, 61 + (k % 4), 3, k, rule=RULE_TRAPEZOID)
+             for k in range(200)]
+    refs = []
+    for d in insts:
+        p = orc.OracleProblem(d["x"], d["f0"], d["ds"], d["nsteps"], rule=d["rule"])
+        refs.append(oracle.propagate(p, d["w0"]))
+    with api.Batch(insts) as b:
+        for prec, tol in ((F32, 1e-5), (F64, 2e-10)):
+            b.evaluate(prec)
+            _, phi, Q = b.get()
+            assert not np.any(b.status() & ST_WATCHDOG), prec
+            for i, (phi_ref, q_ref) in enumerate(refs):
                 assert rel(phi[i], phi_ref) <= tol, (prec, i, rel(phi[i], phi_ref))
                 assert abs(Q[i] - q_ref) <= tol * abs(q_ref), (prec, i)
