@@ -15,8 +15,8 @@
 //   group level : the NW warp separators form a tridiagonal system solved
 //                 redundantly by every warp (PCR with shuffles); two named
 //                 barriers per step exchange the warp-boundary values (on
-//                 thread-block clusters: one CTA barrier and st.async stores
-//                 completing on mbarriers, see cx_*).
+//                 thread-block clusters: st.async stores completing on
+//                 mbarriers, one exchange per step, see cx_*).
 //
 // The density phi_i = sum_k W_k q_k,i q_{nsteps-k},i (romint.c:21-57 Romberg
 // weights, or the trapezoid of simple_FEM_1D_transient.m:119-124) is accumulated
@@ -107,36 +107,35 @@ struct GroupSmem {
   R qw[16];
   int item;
   // Cluster classes only: the per-step exchange between the CTAs of a cluster
-  // (see cx_* below).  x_next: the next CTA's first warp's (zc0, zw); x_R: every
-  // warp's level-2 right-hand side, double-buffered by step parity; xbar: the
-  // mbarriers their remote stores complete on (x_next, x_R parity 0, parity 1).
-  R x_next[2];
-  R x_R[2][NW];
-  unsigned long long xbar[3];
+  // (see cx_* below), double-buffered by step parity: every warp's A_w, zc0_w
+  // and zw_w; per pass, every warp's coefficients of its level-2 right-hand
+  // side on the next warp's values; the mbarriers the remote stores complete
+  // on (parity 0, 1).
+  R x_A[2][NW], x_Z0[2][NW], x_ZW[2][NW];
+  R c_dus[NW], c_ga[NW];
+  unsigned long long xbar[2];
   unsigned xk;  // exchange steps taken by this CTA (all instances so far)
   int xfail;    // a bounded exchange wait ran out (the cluster's results are void)
 };
 
 // Per-step exchange of the cluster classes.  Instead of two cluster barriers
 // per contour step (each a release/acquire of the distributed-shared-memory
-// stores by all CTAs), values move by st.async into the consumer CTA's shared
-// memory and complete on an mbarrier there (transaction bytes), so a consumer
-// waits only for the bytes it reads:
-//   * (zc0, zw) of a warp go to the previous warp: within a CTA through shared
-//     memory and one CTA barrier, across CTAs (first warp of CTA r to the last
-//     warp of CTA r - 1) by st.async on x_next / xbar[0];
-//   * each warp's level-2 right-hand side goes to every CTA's x_R[parity] /
-//     xbar[1 + parity].
+// stores by all CTAs), values move by st.async into every CTA's shared memory
+// and complete on an mbarrier there (transaction bytes), so a CTA waits only
+// for the bytes it reads, once per step.  Warp w's level-2 right-hand side is
+// affine in the next warp's first-lane values:
+//   R_w = A_w - dus_w zc0_{w+1} - ga_w zw_{w+1},  A_w = rl - dls zcl - al zw30
+// (lane 31's terms), so each warp sends A_w, zc0_w and zw_w to every CTA and
+// each lane l < NW forms R_l itself from the per-pass coefficients dus_l, ga_l.
 // Ordering: a warp sends step k+1's values only after the step-k exchange of
-// its own CTA completed, which needs every warp's step-k right-hand side, which
-// each warp produces after reading its step-k inputs; so x_next and its
-// mbarrier need one buffer, while x_R, written by warps of other CTAs that may
-// be one step ahead of a reader, needs two.  Each phase is armed (expected
-// bytes) by one thread of the consumer CTA after it saw the previous phase
-// complete; bytes that arrive before the arming count toward the armed phase.
-// Every wait is bounded: after CX_WAIT_NS the thread marks every CTA of the
-// cluster failed, and from then on the CTAs skip the exchange (no send, no
-// wait, no arming), finish the same steps and report ST_WATCHDOG.
+// its own CTA completed, which needs every warp's step-k values, which each
+// warp sends after reading its step-(k-1) inputs; so two buffers (step parity)
+// suffice.  Each phase is armed (expected bytes) by thread 0 of the consumer
+// CTA right after it saw the previous phase of that buffer complete, before
+// its warp can send the values that let any warp reach the next use.  Every
+// wait is bounded: after CX_WAIT_NS the thread marks every CTA of the cluster
+// failed, and from then on the CTAs skip the exchange (no send, no wait, no
+// arming), finish the same steps and report ST_WATCHDOG.
 #ifndef CX_WAIT_NS
 #define CX_WAIT_NS 1000000000ull
 #endif
@@ -732,15 +731,18 @@ struct Propagator {
     const R r_dls = (R)dls, r_dus = (R)dus, r_vcn = (R)vcn, r_wcn = (R)wcn;
     const bool last_chunk = (P == T - 1);
 
-    // Cluster classes: this CTA's rank in the cluster, the warp's index within
-    // the CTA, the exchange steps taken so far and whether the exchange failed.
-    constexpr int WPC = NW / CL;  // warps per CTA
-    const int xrank = P / CTA, xwl = wid % WPC;
+    // Cluster classes: the exchange steps taken so far, whether the exchange
+    // failed, and lane l's coefficients of warp l's right-hand side on warp
+    // l+1's values (C == 1: no zc0 term).
     unsigned xk = 0;
     bool xbad = false;
+    R xdus = (R)0, xga = (R)0;
     if constexpr (CL > 1) {
       xk = S.xk;
       xbad = S.xfail != 0;
+      if (lane == 31) { put(S.c_dus[wid], (C > 1) ? r_dus : (R)0); put(S.c_ga[wid], r_ga); }
+      gsync(bar_id);
+      if (lane < NW) { xdus = S.c_dus[lane]; xga = S.c_ga[lane]; }
     }
     // Bounded wait for phase `parity` of one of this CTA's exchange mbarriers.
     auto xwait = [&](unsigned bar, unsigned parity) {
@@ -787,43 +789,36 @@ struct Propagator {
         R t2;
         if constexpr (CL > 1) {
           const unsigned par = xk & 1u;
-          if (lane == 0) {
-            S.pub_zc0[wid] = zc0;
-            S.pub_zw[wid] = zw;
-            if (xwl == 0 && xrank > 0 && !xbad) {  // to the last warp of the previous CTA
-              const unsigned rb = cx_remote(cx_smem(&S.xbar[0]), xrank - 1);
-              cx_send(cx_remote(cx_smem(&S.x_next[0]), xrank - 1), zc0, rb);
-              cx_send(cx_remote(cx_smem(&S.x_next[1]), xrank - 1), zw, rb);
-            }
-          }
-          group_sync(bar_id, CTA);
-          if (lane == 31) {
-            R zcx = (R)0;
-            if (wid + 1 < NW) {
-              if (xwl + 1 < WPC) {
-                zcx = S.pub_zc0[wid + 1];
-                zwn = S.pub_zw[wid + 1];
-              } else {
-                xwait(cx_smem(&S.xbar[0]), par);
-                if (!xbad) cx_arm(cx_smem(&S.xbar[0]), 2 * sizeof(R));
-                zcx = S.x_next[0];
-                zwn = S.x_next[1];
+          if (!xbad) {
+            if (lane == 0) {
+#pragma unroll
+              for (int r = 0; r < CL; r++) {
+                const unsigned rb = cx_remote(cx_smem(&S.xbar[par]), r);
+                cx_send(cx_remote(cx_smem(&S.x_Z0[par][wid]), r), zc0, rb);
+                cx_send(cx_remote(cx_smem(&S.x_ZW[par][wid]), r), zw, rb);
               }
-            }
-            if (C > 1) {
-              zc0n = zcx;
-              rho = fmaR(-r_dus, zcx, fmaR(-r_dls, zcl, rl));
-            }
-            const R rw = fmaR(-r_ga, zwn, fmaR(-r_al, zw30, rho));
-            if (!xbad) {
+            } else if (lane == 31) {
+              const R A = fmaR(-r_al, zw30, (C > 1) ? fmaR(-r_dls, zcl, rl) : rl);
 #pragma unroll
               for (int r = 0; r < CL; r++)
-                cx_send(cx_remote(cx_smem(&S.x_R[par][wid]), r), rw, cx_remote(cx_smem(&S.xbar[1 + par]), r));
+                cx_send(cx_remote(cx_smem(&S.x_A[par][wid]), r), A, cx_remote(cx_smem(&S.xbar[par]), r));
             }
           }
-          xwait(cx_smem(&S.xbar[1 + par]), (xk >> 1) & 1u);
-          if (threadIdx.x == 0 && !xbad) cx_arm(cx_smem(&S.xbar[1 + par]), NW * sizeof(R));
-          t2 = (lane < NW) ? S.x_R[par][lane] : (R)0;
+          xwait(cx_smem(&S.xbar[par]), (xk >> 1) & 1u);
+          if (threadIdx.x == 0 && !xbad) cx_arm(cx_smem(&S.xbar[par]), 3 * NW * sizeof(R));
+          // lane l < NW: warp l's right-hand side (the last warp has no next)
+          const int ln = min(lane + 1, NW - 1), la = min(lane, NW - 1);
+          const bool nx = lane + 1 < NW;
+          const R z0n = nx ? S.x_Z0[par][ln] : (R)0, zwl = nx ? S.x_ZW[par][ln] : (R)0;
+          const R rA = S.x_A[par][la];
+          t2 = (lane < NW) ? fmaR(-xga, zwl, fmaR(-xdus, z0n, rA)) : (R)0;
+          if (lane == 31) {  // the next warp's first-lane values (zero after the last warp)
+            const int wn = min(wid + 1, NW - 1);
+            const bool hn = wid + 1 < NW;
+            const R zcx = hn ? S.x_Z0[par][wn] : (R)0;
+            zwn = hn ? S.x_ZW[par][wn] : (R)0;
+            if (C > 1) zc0n = zcx;
+          }
           xk++;
         } else {
           if (lane == 0) { put(S.pub_zc0[wid], zc0); put(S.pub_zw[wid], zw); }
@@ -1049,13 +1044,10 @@ __global__ void __launch_bounds__(32 * NW / CL, 1) propagate_cluster_kernel(Batc
   if (threadIdx.x == 0) {
     sm.xk = 0;
     sm.xfail = 0;
-    for (int i = 0; i < 3; i++) cx_init(cx_smem(&sm.xbar[i]));
+    for (int i = 0; i < 2; i++) cx_init(cx_smem(&sm.xbar[i]));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    // first phases: the next CTA's (zc0, zw) (not on the last CTA, which has
-    // no next), every warp's right-hand side for each step parity
-    if (rank + 1 < CL) cx_arm(cx_smem(&sm.xbar[0]), 2 * sizeof(R));
-    cx_arm(cx_smem(&sm.xbar[1]), NW * sizeof(R));
-    cx_arm(cx_smem(&sm.xbar[2]), NW * sizeof(R));
+    // first phase of each step parity: every warp's A, zc0 and zw
+    for (int i = 0; i < 2; i++) cx_arm(cx_smem(&sm.xbar[i]), 3 * NW * sizeof(R));
   }
   cooperative_groups::this_cluster().sync();  // barriers initialised before any remote store
   Pp::run(b, cls, sm, P, worker, 1);
