@@ -248,6 +248,13 @@ def solve_opts(**kw) -> L.ScftSolveOpts:
     return o
 
 
+def _results(res) -> dict:
+    """The scft_result array as one numpy array per field (a structured view of
+    the ctypes array, copied)."""
+    a = np.ctypeslib.as_array(res)
+    return {k: a[k].copy() for k in ("status", "iterations", "err", "Q")}
+
+
 class Batch:
     """Independent SCFT instances solved together on the GPU.
 
@@ -262,6 +269,7 @@ class Batch:
         self.count = len(a["n_nodes"])
         self.n_nodes = a["n_nodes"]
         self.offsets = np.concatenate([[0], np.cumsum(self.n_nodes)])
+        self._bounds = list(zip(self.offsets[:-1].tolist(), self.offsets[1:].tolist()))
         desc = Batch._descriptors(a, self.offsets)
         self._keep = [a]
         h = C.c_void_p()
@@ -326,7 +334,7 @@ class Batch:
         return desc
 
     def split(self, flat):
-        return [flat[self.offsets[i]:self.offsets[i + 1]] for i in range(self.count)]
+        return [flat[a:z] for a, z in self._bounds]
 
     def set_fields(self, w_nodes_list):
         flat = np.ascontiguousarray(np.concatenate(w_nodes_list), dtype=np.float64)
@@ -344,12 +352,7 @@ class Batch:
         o = opts if opts is not None else solve_opts(**kw)
         res = (L.ScftResult * self.count)()
         check(self.lib.scft_batch_solve(self.h, C.byref(o), res), "scft_batch_solve")
-        return {
-            "status": np.array([r.status for r in res]),
-            "iterations": np.array([r.iterations for r in res]),
-            "err": np.array([r.err for r in res]),
-            "Q": np.array([r.Q for r in res]),
-        }
+        return _results(res)
 
     def solve_async(self, opts: L.ScftSolveOpts | None = None, **kw):
         """Enqueue the fused FP32 solve and return at once; wait() completes it.
@@ -360,12 +363,7 @@ class Batch:
     def wait(self):
         res = (L.ScftResult * self.count)()
         check(self.lib.scft_batch_wait(self.h, res), "scft_batch_wait")
-        return {
-            "status": np.array([r.status for r in res]),
-            "iterations": np.array([r.iterations for r in res]),
-            "err": np.array([r.err for r in res]),
-            "Q": np.array([r.Q for r in res]),
-        }
+        return _results(res)
 
     def get(self):
         tot = int(self.offsets[-1])

@@ -12,8 +12,8 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libscft.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"),
-         "--expt-relaxed-constexpr"]
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread",
+         "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
 
 
 def sources():
@@ -50,7 +50,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         list(ex.map(run, cmds))
     if cmds or not os.path.exists(LIB):
-        run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+        run([nvcc, *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", LIB, *objs, "-lcudart", "-lpthread"])
     return LIB
 
 

@@ -18,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -619,6 +620,22 @@ static void destroy_batch(scft_batch *B) {
   delete B;
 }
 
+// Host work over [0, n) split across up to 8 threads when there is enough of
+// it (packing and unpacking the batch arrays): f(begin, end) on each share.
+template <typename F>
+static void host_parallel(long long n, long long grain, F f) {
+  const long long hw = std::max(1u, std::thread::hardware_concurrency());
+  const int T = (int)std::min<long long>(std::min<long long>(8, hw), std::max(1LL, n / std::max(1LL, grain)));
+  if (T <= 1) {
+    f(0LL, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; t++) th.emplace_back(f, n * t / T, n * (t + 1) / T);
+  f(0LL, n / T);
+  for (auto &x : th) x.join();
+}
+
 static int create_batch(const scft_instance *inst, int count, scft_batch **out) {
   if (!inst || count <= 0 || !out) return set_err(SCFT_EINVAL, "batch: no instances");
   int ndev = 0;
@@ -631,35 +648,50 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
   B->n.resize(count); B->nsteps.resize(count); B->rule.resize(count); B->ds.resize(count);
   B->node_off.resize(count); B->int_off.resize(count); B->spacing_ratio.resize(count); B->width.resize(count);
   for (int p = 0; p < 2; p++) { B->shapeC[p].assign(count, 0); B->shapeNW[p].assign(count, 0); }
+  // per instance (in parallel): validity, spacing ratio, width; 0 or the
+  // error (1 description, 2 Romberg step count, 3 mesh order)
+  std::vector<int> bad(count, 0);
+  host_parallel(count, 256, [&](long long i0, long long i1) {
+    for (long long i = i0; i < i1; i++) {
+      const scft_instance &s = inst[i];
+      if (s.n_nodes < 3 || s.nsteps < 1 || !(s.ds > 0.0) || !s.f0 ||
+          (s.rule != SCFT_RULE_ROMBERG && s.rule != SCFT_RULE_TRAPEZOID) || (!s.x && !(s.L > 0.0))) {
+        bad[i] = 1;
+        continue;
+      }
+      double qw[16];
+      if (quad_table(s.nsteps, s.ds, s.rule, qw)) {
+        bad[i] = 2;
+        continue;
+      }
+      double hmin = 1.0, hmax = 1.0;  // uniform when x is not given
+      if (s.x) {
+        hmin = INFINITY;
+        hmax = 0.0;
+        for (int k = 1; k < s.n_nodes; k++) {
+          const double h = s.x[k] - s.x[k - 1];
+          if (!(h > 0.0)) {
+            bad[i] = 3;
+            break;
+          }
+          hmin = std::min(hmin, h);
+          hmax = std::max(hmax, h);
+        }
+        if (bad[i]) continue;
+      }
+      B->spacing_ratio[i] = hmax / hmin;
+      B->width[i] = s.x ? s.x[s.n_nodes - 1] - s.x[0] : s.L;
+    }
+  });
   long long no = 0, io = 0;
   for (int i = 0; i < count; i++) {
+    if (bad[i]) {
+      destroy_batch(B);
+      if (bad[i] == 1) return set_err(SCFT_EINVAL, "instance %d: invalid description", i);
+      if (bad[i] == 2) return set_err(SCFT_EINVAL, "instance %d: Romberg needs a power-of-two step count >= 16", i);
+      return set_err(SCFT_EINVAL, "instance %d: mesh not strictly increasing", i);
+    }
     const scft_instance &s = inst[i];
-    if (s.n_nodes < 3 || s.nsteps < 1 || !(s.ds > 0.0) || !s.f0 ||
-        (s.rule != SCFT_RULE_ROMBERG && s.rule != SCFT_RULE_TRAPEZOID) || (!s.x && !(s.L > 0.0))) {
-      destroy_batch(B);
-      return set_err(SCFT_EINVAL, "instance %d: invalid description", i);
-    }
-    double qw[16];
-    if (quad_table(s.nsteps, s.ds, s.rule, qw)) {
-      destroy_batch(B);
-      return set_err(SCFT_EINVAL, "instance %d: Romberg needs a power-of-two step count >= 16", i);
-    }
-    double hmin = 1.0, hmax = 1.0;  // uniform when x is not given
-    if (s.x) {
-      hmin = INFINITY;
-      hmax = 0.0;
-      for (int k = 1; k < s.n_nodes; k++) {
-        const double h = s.x[k] - s.x[k - 1];
-        if (!(h > 0.0)) {
-          destroy_batch(B);
-          return set_err(SCFT_EINVAL, "instance %d: mesh not strictly increasing", i);
-        }
-        hmin = std::min(hmin, h);
-        hmax = std::max(hmax, h);
-      }
-    }
-    B->spacing_ratio[i] = hmax / hmin;
-    B->width[i] = s.x ? s.x[s.n_nodes - 1] - s.x[0] : s.L;
     B->n[i] = s.n_nodes; B->nsteps[i] = s.nsteps; B->rule[i] = s.rule; B->ds[i] = s.ds;
     B->node_off[i] = no; B->int_off[i] = io;
     no += s.n_nodes; io += s.n_nodes - 2;
@@ -692,23 +724,26 @@ static int create_batch(const scft_instance *inst, int count, scft_batch **out) 
   double *hx = stage, *hf = hx + nd, *hw = hf + nd, *hqw = hw + nd, *hds = hqw + 16 * nc, *hsp = hds + nc;
   long long *hno = reinterpret_cast<long long *>(hsp + nc), *hio = hno + nc;
   int *hn = reinterpret_cast<int *>(hio + nc), *hns = hn + nc;
-  for (int i = 0; i < count; i++) {
-    const scft_instance &s = inst[i];
-    const long long o = B->node_off[i];
-    for (int k = 0; k < s.n_nodes; k++) {
-      hx[o + k] = s.x ? s.x[k] : s.L * (double)k / (double)(s.n_nodes - 1);
-      hf[o + k] = s.f0[k];
-      hw[o + k] = s.w0 ? s.w0[k] : 0.0;
+  host_parallel(count, 256, [&](long long i0, long long i1) {
+    for (long long i = i0; i < i1; i++) {
+      const scft_instance &s = inst[i];
+      const long long o = B->node_off[i];
+      if (s.x) std::memcpy(hx + o, s.x, s.n_nodes * sizeof(double));
+      else
+        for (int k = 0; k < s.n_nodes; k++) hx[o + k] = s.L * (double)k / (double)(s.n_nodes - 1);
+      std::memcpy(hf + o, s.f0, s.n_nodes * sizeof(double));
+      if (s.w0) std::memcpy(hw + o, s.w0, s.n_nodes * sizeof(double));
+      else std::memset(hw + o, 0, s.n_nodes * sizeof(double));
+      if (!s.x) hx[o + s.n_nodes - 1] = s.L;
+      quad_table(s.nsteps, s.ds, s.rule, hqw + 16 * (size_t)i);
+      hds[i] = s.ds;
+      hsp[i] = B->spacing_ratio[i];
+      hno[i] = o;
+      hio[i] = B->int_off[i];
+      hn[i] = s.n_nodes;
+      hns[i] = s.nsteps;
     }
-    if (!s.x) hx[o + s.n_nodes - 1] = s.L;
-    quad_table(s.nsteps, s.ds, s.rule, hqw + 16 * (size_t)i);
-    hds[i] = s.ds;
-    hsp[i] = B->spacing_ratio[i];
-    hno[i] = o;
-    hio[i] = B->int_off[i];
-    hn[i] = s.n_nodes;
-    hns[i] = s.nsteps;
-  }
+  });
   cudaStream_t st = B->st;
   struct Cp { void *d; const void *h; size_t bytes; } cps[] = {
       {B->d_n, hn, nc * sizeof(int)},
