@@ -181,7 +181,8 @@ struct Log2<1> { static constexpr int v = 0; };
 // 32*NW/CL threads each (large shapes, whose 32*NW threads would otherwise get
 // too few registers per thread in one CTA).  Group-level values are written to
 // the shared memory of every CTA of the cluster (distributed shared memory) and
-// read locally; the group barrier is the cluster barrier.
+// read locally; outside the contour loop the group barrier is the cluster
+// barrier, inside it the per-step exchange is st.async on mbarriers (cx_*).
 template <typename R, int C, int NW, bool DELTA, int CL = 1>
 struct Propagator {
   static constexpr int T = 32 * NW;
