@@ -31,7 +31,10 @@ extern "C" {
 #define SCFT_ST_CONVERGED 4
 #define SCFT_ST_MAXIT 8
 #define SCFT_ST_RESTARTED 16   /* the Anderson history was restarted at least once */
-#define SCFT_ST_WATCHDOG 32    /* the host loop stopped on its launch cap */
+#define SCFT_ST_WATCHDOG 32    /* stopped by a bound: the host loop's launch cap, the solve's time
+                                  budget (budget_ms), or (shapes on thread-block clusters) a
+                                  per-step exchange wait between the cluster's CTAs that ran out,
+                                  which voids that pass's density */
 #define SCFT_ST_FP64 64        /* the FP32 iteration stalled and the FP64 propagator finished the solve */
 #define SCFT_ST_FORKED 128     /* the result comes from a forked path of the mixing (scft_solve_opts.forks) */
 #define SCFT_MAX_FORKS 4
