@@ -240,7 +240,10 @@ typedef struct scft_batch scft_batch;
 
 void scft_solve_opts_init(scft_solve_opts *o);
 
-/* Copies the instances to the device.  Returns SCFT_OK and *out, or an error. */
+/* Copies the instances to the device.  Returns SCFT_OK and *out, or an error
+   (the lowest invalid instance is named).  Large batches are checked and packed
+   into one pinned upload buffer by up to 8 host threads that end before the
+   call returns; the caller's arrays are only read, and may be reused at once. */
 int scft_batch_create(const scft_instance *inst, int count, scft_batch **out);
 /* Overwrite all fields (concatenated n_nodes values per instance; wall values
    are kept for the free energy, the propagator ignores them). */
